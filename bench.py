@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 field-line tracer, one JSON line on rank 0.
+
+A step is one trace of the GPU-scale workload: 4096 charges uniform in
+[-100,100]^3 with |q| in U[1,10] and random sign, 16 lines seeded per
+positive charge on a radius-1 Fibonacci sphere, 5000 rows per line, the
+reference's curvature stepping rule (CalcField_CPU_T_Curvature, SSE form).
+  value  pair interactions/s with inputs resident in HBM (device pointers)
+  e2e    the same through the host-pointer C ABI call (em_calc_field_ex_f32):
+         seeds and charges copied in, all vertices copied out, every step
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port of CPU_Implement.cpp, OpenMP over all host cores) on bounded
+samples of the same workload.
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+METRIC = ("Gpair-int/s vs plain FP32 at ≤1e-6 field err vs FP64; "
+          "adjoint/fwd time ratio")
+UNIT = "Gpair-int/s"
+FLOP_PER_PAIR = 20  # the FP32-roofline credit per pair interaction
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="gpu_4096")
+    ap.add_argument("--rows", type=int, default=None,
+                    help="override rows per line (quick runs only)")
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(em, name, seed, rows):
+    ch, seeds, steps = em.workloads.make(name, seed=seed)
+    if rows:
+        steps = rows
+    return np.ascontiguousarray(ch, np.float32), seeds.astype(np.float32), steps
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_rate(orc, ch, seeds, rows, seconds, nthreads):
+    """Oracle port on host cores over a bounded sample: all charges, a
+    line subset and a row count sized to take about `seconds`."""
+    # the reference's SSE path needs n % 64 == 0 (CPU_Implement.cpp:223);
+    # pad with copies of seed 0 as a reference user would
+    seeds = np.concatenate([seeds, np.repeat(seeds[:1], (-len(seeds)) % 64, 0)])
+    n = len(seeds)
+    p = len(ch)
+    # calibrate on a small sample
+    lines = min(n, 256)
+    cal_rows = 4
+    x = np.zeros(n * cal_rows, np.float32)
+    xs = [x.copy(), x.copy(), x.copy()]
+    for c in range(3):
+        xs[c][:n] = seeds[:, c]
+    t = time.perf_counter()
+    orc.calc_field(*xs, ch, n, 1.0, orc.CURV_SSE, 0, lines, nthreads)
+    dt = max(time.perf_counter() - t, 1e-4)
+    rate = lines * (cal_rows - 1) * p / dt
+    want_pairs = rate * seconds
+    lines = int(min(n, max(64, want_pairs / (p * max(rows - 1, 1)))))
+    lines = max(64, lines // 64 * 64) if n >= 64 else n
+    srows = int(min(rows, max(2, want_pairs / (lines * p) + 1)))
+    xs = [np.zeros(n * srows, np.float32) for _ in range(3)]
+    for c in range(3):
+        xs[c][:n] = seeds[:, c]
+    t = time.perf_counter()
+    rc = orc.calc_field(*xs, ch, n, 1.0, orc.CURV_SSE, 0, lines, nthreads)
+    dt = time.perf_counter() - t
+    if rc:
+        raise RuntimeError(f"oracle returned {rc}")
+    pairs = lines * (srows - 1) * p
+    return pairs / dt / 1e9, dict(lines=lines, rows=srows, pairs=pairs,
+                                  seconds=dt)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    em = importlib.import_module("electromag-with-cuda_gb300")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import em_oracle as orc
+    ch, seeds, rows = workload(em, args.workload, args.seed, args.rows)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_rate(orc, ch, seeds, rows, min(per_step, 2.0), threads)
+    vals, sample = [], None
+    for _ in range(args.steps):
+        v, sample = cpu_rate(orc, ch, seeds, rows, per_step, threads)
+        vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sample["seconds"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "lines": int(len(seeds)),
+                   "charges": int(len(ch)), "rows": int(rows),
+                   "rule": "curvature, seed vector (CPU_Implement.cpp:207-351)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                         "kind": "port",
+                         "sample": f"{sample['lines']} lines x {len(ch)} charges"
+                                   f" x {sample['rows']} rows per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    em = importlib.import_module("electromag-with-cuda_gb300")
+    lib = em.load()
+    ch, seeds, rows = workload(em, args.workload, args.seed + 0, args.rows)
+    n, p = len(seeds), len(ch)
+    pairs = float(n) * (rows - 1) * p
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    X = [torch.zeros(n * rows, dtype=torch.float32, device=dev) for _ in range(3)]
+    for c in range(3):
+        X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c])).to(dev)
+    dch = torch.from_numpy(ch).to(dev)
+
+    def step():
+        rc, perf = em.calc_field(*X, dch, n, 1.0, True, require_n64=False,
+                                 stream=stream.cuda_stream)
+        if rc:
+            raise em.EmError(rc, "em_calc_field_ex_f32")
+        return perf
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    peak_tflops = lib_peak(lib)
+    barrier()
+    launches0 = lib.em_launch_count()
+    kern = []
+    with ClockSampler(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        t0.record(stream)
+        for _ in range(args.steps):
+            kern.append(step().time)
+        t1.record(stream)
+        barrier()
+    launches = lib.em_launch_count() - launches0
+    ms = t0.elapsed_time(t1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = pairs * world * args.steps / (ms * 1e-3) / 1e9
+    kernel_s = float(np.mean(kern))
+    achieved = FLOP_PER_PAIR * pairs / kernel_s / 1e12
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(em, torch, dist, ch, seeds, rows, args, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import em_oracle as orc
+        threads = os.cpu_count() or 1
+        v, smp = cpu_rate(orc, ch, seeds, rows, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{smp['lines']} of {n} lines x {p} charges x "
+                         f"{smp['rows']} rows ({smp['seconds']:.1f} s)"}
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG64)",
+        "config": {"workload": args.workload, "lines": n, "charges": p,
+                   "rows": rows, "seed": args.seed,
+                   "rule": "curvature, seed vector (CPU_Implement.cpp:207-351)",
+                   "arith": "fast FP32 (rsqrt + FMA)",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "vertex output %.2f GB per step exceeds the 129 MB L2"
+                         % (3 * 4 * n * rows / 1e9)},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops,
+                     "unit": "TFLOP/s", "frac": achieved / peak_tflops,
+                     "traffic": None,
+                     "peak_source": "measured FFMA peak (em_fp32_peak_tflops)",
+                     "flop_per_pair": FLOP_PER_PAIR,
+                     "kernel_ms": kernel_s * 1e3},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def lib_peak(lib):
+    import ctypes
+    t = ctypes.c_double()
+    s = ctypes.c_double()
+    rc = lib.em_fp32_peak_tflops(ctypes.byref(t), ctypes.byref(s))
+    if rc:
+        raise RuntimeError(f"em_fp32_peak_tflops failed: {rc}")
+    return t.value
+
+
+def run_e2e(em, torch, dist, ch, seeds, rows, args, world):
+    """Host-pointer C ABI calls on pinned buffers: seeds and charges go in,
+    every vertex comes out, each step."""
+    n, p = len(seeds), len(ch)
+    H = [torch.zeros(n * rows, dtype=torch.float32).pin_memory()
+         for _ in range(3)]
+    hch = torch.from_numpy(ch).pin_memory()
+    Hn = [h.numpy() for h in H]
+    for c in range(3):
+        Hn[c][:n] = seeds[:, c]
+    chn = hch.numpy()
+
+    def step():
+        rc, _ = em.calc_field(*Hn, chn, n, 1.0, True, require_n64=False,
+                              plain=False)
+        if rc:
+            raise em.EmError(rc, "em_calc_field_ex_f32 (host)")
+
+    step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sec = time.perf_counter() - t
+    if dist:
+        tt = torch.tensor([sec], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        sec = float(tt.item())
+    pairs = float(n) * (rows - 1) * p * world * args.steps
+    return {"value": pairs / sec / 1e9, "unit": UNIT,
+            "h2d_bytes_per_step": 3 * 4 * n + 16 * p,
+            "d2h_bytes_per_step": 3 * 4 * n * (rows - 1) + 4}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,11 @@
+"""GB300-native field-line tracer for ElectroMag (libemgb300.so + bindings).
+
+Import with importlib (the directory name carries hyphens):
+    em = importlib.import_module("electromag-with-cuda_gb300")
+"""
+from . import _capi, tracer, workloads  # noqa: F401
+from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
+from .tracer import calc_field, field, new_lines  # noqa: F401
+
+__all__ = ["calc_field", "field", "new_lines", "load", "declared_symbols", "strerror",
+           "EmError", "workloads"]

@@ -1,0 +1,388 @@
+// C ABI of libemgb300.so: argument checks in the reference's order, device
+// buffers cached per device, launch planning, host<->device staging.
+//
+// Return codes 1/2/3/5 and their order follow CPU_Implement.cpp:213-230.
+// The _f32/_f64 entry points take host pointers and return when the result
+// is in the caller's arrays, like CalcField_CPU<T> (CPU_Implement.cpp:501).
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstring>
+#include <mutex>
+
+#include "em_internal.h"
+#include "emgb300.h"
+#include "em_plan.h"
+
+namespace em {
+
+DevCtx *get_ctx(int *code)
+{
+    static DevCtx ctxs[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        *code = EM_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    DevCtx &c = ctxs[dev];
+    std::lock_guard<std::mutex> g(c.init_mu);
+    if (!c.ready) {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+            cudaGetLastError();
+            *code = EM_ERR_NO_DEVICE;
+            return nullptr;
+        }
+        c.device = dev;
+        c.nsm = prop.multiProcessorCount;
+        c.smem_optin = prop.sharedMemPerBlockOptin;
+        if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&c.ev0) != cudaSuccess || cudaEventCreate(&c.ev1) != cudaSuccess) {
+            cudaGetLastError();
+            *code = EM_ERR_CUDA;
+            return nullptr;
+        }
+        c.ready = true;
+    }
+    *code = EM_OK;
+    return &c;
+}
+
+int grow(void **buf, size_t *cap, size_t need)
+{
+    if (need <= *cap && *buf)
+        return EM_OK;
+    if (*buf) {
+        cudaFree(*buf);
+        *buf = nullptr;
+        *cap = 0;
+    }
+    const size_t want = std::max<size_t>(need, 256);
+    if (cudaMalloc(buf, want) != cudaSuccess) {
+        cudaGetLastError();
+        *buf = nullptr;
+        return EM_ERR_NOMEM;
+    }
+    *cap = want;
+    return EM_OK;
+}
+
+int map_cuda(cudaError_t e)
+{
+    if (e == cudaSuccess)
+        return EM_OK;
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? EM_ERR_NOMEM : EM_ERR_CUDA;
+}
+
+int read_dev_err(DevCtx &c, cudaStream_t s, int *dev_err_host)
+{
+    int v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, c.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return map_cuda(e);
+    *dev_err_host = v;
+    return v == EM_DEVERR_TIMEOUT ? EM_ERR_TIMEOUT : (v ? EM_ERR_CUDA : EM_OK);
+}
+
+namespace {
+
+template <class T>
+int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges, size_t p,
+               T resolution, int use_curvature, const em_options *opt, bool plain,
+               em_perf *perf)
+{
+    using clock = std::chrono::steady_clock;
+    const auto t_start = clock::now();
+    // Reference order of checks: CPU_Implement.cpp:213-230.
+    if (!n)
+        return EM_ERR_N_ZERO;
+    if (resolution == 0)
+        return EM_ERR_RESOLUTION;
+    const bool req64 = plain ? true : (opt && opt->require_n64);
+    if (use_curvature && req64 && (n & 63))
+        return EM_ERR_N_ALIGN;
+    if (total_steps < 2)
+        return EM_ERR_STEPS;
+    if (!x || !y || !z || (p && !charges))
+        return EM_ERR_ARG;
+    em_options o{};
+    if (opt)
+        o = *opt;
+    if (o.arith != EM_ARITH_FAST && o.arith != EM_ARITH_EXACT)
+        return EM_ERR_ARG;
+    if (o.rule != EM_RULE_SSE && o.rule != EM_RULE_GENERIC)
+        return EM_ERR_ARG;
+    if (total_steps > (size_t)INT_MAX || p > (size_t)(INT_MAX / 64) ||
+        n > (size_t)(LLONG_MAX / 64) / total_steps)
+        return EM_ERR_TOO_LARGE;
+    if (o.device_ptrs && ((uintptr_t)charges & 15))
+        return EM_ERR_ARG;
+    if (perf)
+        perf->progress = 0;
+
+    int code = EM_OK;
+    DevCtx *cp = get_ctx(&code);
+    if (!cp)
+        return code;
+    DevCtx &c = *cp;
+    std::lock_guard<std::mutex> guard(c.mu);
+
+    Plan pl;
+    code = make_plan<T>(c, n, p, o, &pl);
+    if (code)
+        return code;
+    const size_t rec = sizeof(T) * 4;
+    cudaStream_t s = (o.device_ptrs && o.stream) ? (cudaStream_t)o.stream : c.stream;
+
+    if ((code = grow(&c.charges, &c.charges_cap, (size_t)pl.p_pad * rec)))
+        return code;
+    if ((code = grow(&c.errbuf, &c.errbuf_cap, 256)))
+        return code;
+    c.err = static_cast<int *>(c.errbuf);
+
+    T *dx = x, *dy = y, *dz = z;
+    const size_t elems = n * total_steps;
+    if (!o.device_ptrs) {
+        if ((code = grow(&c.lines, &c.lines_cap, 3 * elems * sizeof(T))))
+            return code;
+        dx = static_cast<T *>(c.lines);
+        dy = dx + elems;
+        dz = dy + elems;
+    }
+    cudaError_t e = cudaSuccess;
+    const cudaMemcpyKind kin = o.device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (p)
+        e = cudaMemcpyAsync(c.charges, charges, p * rec, kin, s);
+    if (e == cudaSuccess)
+        e = launch_pad_charges<T>(c.charges, (int)p, pl.p_pad, s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(c.err, 0, sizeof(int), s);
+    if (e == cudaSuccess && !o.device_ptrs) {
+        e = cudaMemcpyAsync(dx, x, n * sizeof(T), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dy, y, n * sizeof(T), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dz, z, n * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+    if (e != cudaSuccess)
+        return map_cuda(e);
+
+    RefTraceParams<T> prm{};
+    prm.x = dx;
+    prm.y = dy;
+    prm.z = dz;
+    prm.charges = c.charges;
+    prm.n = (long long)n;
+    prm.n_groups = pl.n_groups;
+    prm.total_steps = (int)total_steps;
+    prm.p_pad = pl.p_pad;
+    prm.n_tiles = pl.n_tiles;
+    prm.tile_recs = pl.cfg.tile_recs;
+    prm.stages = pl.cfg.stages;
+    prm.resident = pl.cfg.resident;
+    prm.rule = use_curvature ? o.rule : RULE_FIXED;
+    prm.resolution = resolution;
+    prm.err = c.err;
+
+    e = cudaEventRecord(c.ev0, s);
+    if (e == cudaSuccess)
+        e = launch_ref_trace<T>(prm, pl.cfg, o.arith, s);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(c.ev1, s);
+    if (e != cudaSuccess)
+        return map_cuda(e);
+    if (!o.device_ptrs) {
+        const size_t rest = elems - n;
+        e = cudaMemcpyAsync(x + n, dx + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(y + n, dy + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(z + n, dz + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess)
+            return map_cuda(e);
+    }
+    int dev_err = 0;
+    code = read_dev_err(c, s, &dev_err);
+    if (code)
+        return code;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    if (perf) {
+        const double tk = ms * 1e-3;
+        perf->time = tk;
+        perf->pairs = (double)n * (double)(total_steps - 1) * (double)p;
+        perf->performance =
+            tk > 0 ? (double)n * (double)(total_steps - 1) * (18.0 * (double)p + 13.0) / tk / 1e9
+                   : 0;
+        perf->wall_time = std::chrono::duration<double>(clock::now() - t_start).count();
+        perf->progress = 1.0;
+    }
+    return EM_OK;
+}
+
+template <class T>
+int field_at(const T *px, const T *py, const T *pz, size_t m, const T *charges, size_t p,
+             T *ex, T *ey, T *ez, const em_options *opt)
+{
+    if (!m)
+        return EM_OK;
+    if (!px || !py || !pz || !ex || !ey || !ez || (p && !charges))
+        return EM_ERR_ARG;
+    if (p > (size_t)INT_MAX / 4 || m > (size_t)LLONG_MAX / 64)
+        return EM_ERR_TOO_LARGE;
+    em_options o{};
+    if (opt)
+        o = *opt;
+    if (o.arith != EM_ARITH_FAST && o.arith != EM_ARITH_EXACT)
+        return EM_ERR_ARG;
+    int code = EM_OK;
+    DevCtx *cp = get_ctx(&code);
+    if (!cp)
+        return code;
+    DevCtx &c = *cp;
+    std::lock_guard<std::mutex> guard(c.mu);
+    cudaStream_t s = (o.device_ptrs && o.stream) ? (cudaStream_t)o.stream : c.stream;
+    const T *dpx = px, *dpy = py, *dpz = pz, *dch = charges;
+    T *dex = ex, *dey = ey, *dez = ez;
+    cudaError_t e = cudaSuccess;
+    if (!o.device_ptrs) {
+        if ((code = grow(&c.scratch, &c.scratch_cap, (6 * m + 4 * p + 64) * sizeof(T))))
+            return code;
+        T *b = static_cast<T *>(c.scratch);
+        T *bpx = b, *bpy = b + m, *bpz = b + 2 * m, *bch = b + 3 * m;
+        dex = bch + 4 * p + 32;
+        dey = dex + m;
+        dez = dey + m;
+        e = cudaMemcpyAsync(bpx, px, m * sizeof(T), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(bpy, py, m * sizeof(T), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(bpz, pz, m * sizeof(T), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && p)
+            e = cudaMemcpyAsync(bch, charges, 4 * p * sizeof(T), cudaMemcpyHostToDevice, s);
+        dpx = bpx;
+        dpy = bpy;
+        dpz = bpz;
+        dch = bch;
+    }
+    if (e == cudaSuccess)
+        e = launch_field<T>(dpx, dpy, dpz, (long long)m, dch, (int)p, o.arith,
+                            o.rule == EM_RULE_SSE, dex, dey, dez, s);
+    if (e == cudaSuccess && !o.device_ptrs) {
+        e = cudaMemcpyAsync(ex, dex, m * sizeof(T), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ey, dey, m * sizeof(T), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ez, dez, m * sizeof(T), cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    return map_cuda(e);
+}
+
+} // namespace
+} // namespace em
+
+extern "C" {
+
+int em_field_f32(const float *px, const float *py, const float *pz, size_t m,
+                 const float *charges, size_t p, float *ex, float *ey, float *ez,
+                 const em_options *opt)
+{
+    return em::field_at<float>(px, py, pz, m, charges, p, ex, ey, ez, opt);
+}
+
+int em_field_f64(const double *px, const double *py, const double *pz, size_t m,
+                 const double *charges, size_t p, double *ex, double *ey, double *ez,
+                 const em_options *opt)
+{
+    return em::field_at<double>(px, py, pz, m, charges, p, ex, ey, ez, opt);
+}
+
+int em_calc_field_f32(float *x, float *y, float *z, size_t n, size_t total_steps,
+                      const float *charges, size_t p, float resolution, int use_curvature,
+                      em_perf *perf)
+{
+    return em::calc_field<float>(x, y, z, n, total_steps, charges, p, resolution,
+                                 use_curvature, nullptr, true, perf);
+}
+
+int em_calc_field_f64(double *x, double *y, double *z, size_t n, size_t total_steps,
+                      const double *charges, size_t p, double resolution, int use_curvature,
+                      em_perf *perf)
+{
+    return em::calc_field<double>(x, y, z, n, total_steps, charges, p, resolution,
+                                  use_curvature, nullptr, true, perf);
+}
+
+int em_calc_field_ex_f32(float *x, float *y, float *z, size_t n, size_t total_steps,
+                         const float *charges, size_t p, float resolution, int use_curvature,
+                         const em_options *opt, em_perf *perf)
+{
+    return em::calc_field<float>(x, y, z, n, total_steps, charges, p, resolution,
+                                 use_curvature, opt, false, perf);
+}
+
+int em_calc_field_ex_f64(double *x, double *y, double *z, size_t n, size_t total_steps,
+                         const double *charges, size_t p, double resolution,
+                         int use_curvature, const em_options *opt, em_perf *perf)
+{
+    return em::calc_field<double>(x, y, z, n, total_steps, charges, p, resolution,
+                                  use_curvature, opt, false, perf);
+}
+
+int em_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int em_release(void)
+{
+    int code = EM_OK;
+    em::DevCtx *c = em::get_ctx(&code);
+    if (!c)
+        return code;
+    std::lock_guard<std::mutex> g(c->mu);
+    for (auto pr : {std::make_pair(&c->charges, &c->charges_cap),
+                    std::make_pair(&c->lines, &c->lines_cap),
+                    std::make_pair(&c->scratch, &c->scratch_cap),
+                    std::make_pair(&c->errbuf, &c->errbuf_cap)}) {
+        if (*pr.first)
+            cudaFree(*pr.first);
+        *pr.first = nullptr;
+        *pr.second = 0;
+    }
+    c->err = nullptr;
+    return EM_OK;
+}
+
+const char *em_strerror(int code)
+{
+    switch (code) {
+    case EM_OK: return "success";
+    case EM_ERR_N_ZERO: return "n == 0";
+    case EM_ERR_RESOLUTION: return "resolution == 0";
+    case EM_ERR_STEPS: return "total_steps < 2";
+    case EM_ERR_ARG: return "invalid argument";
+    case EM_ERR_N_ALIGN: return "n is not a multiple of 64";
+    case EM_ERR_CUDA: return "CUDA runtime error";
+    case EM_ERR_NOMEM: return "device memory allocation failed";
+    case EM_ERR_TIMEOUT: return "device-side wait timed out";
+    case EM_ERR_NO_DEVICE: return "no usable CUDA device";
+    case EM_ERR_TOO_LARGE: return "size beyond this entry point's limit";
+    default: return "unknown error";
+    }
+}
+
+const char *em_version(void) { return "0.1.0"; }
+
+} // extern "C"

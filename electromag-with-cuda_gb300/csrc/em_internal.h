@@ -1,0 +1,90 @@
+// Internal declarations shared by the kernels (.cu) and the C ABI layer.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace em {
+
+// Device error word values (the kernel's status, read back by the host).
+enum DevErr : int {
+    EM_DEVERR_NONE = 0,
+    EM_DEVERR_TIMEOUT = 1, // a bounded wait gave up
+    EM_DEVERR_CONFIG = 2,  // launch parameters inconsistent (checked in-kernel)
+};
+
+// Stepping rules (which reference routine a run reproduces).
+enum Rule : int {
+    RULE_SSE = 0,     // CPU_Implement.cpp:207-351 / :366-498 (curvature, seed vector)
+    RULE_GENERIC = 1, // CPU_Implement.cpp:104-191 (curvature, previous point)
+    RULE_FIXED = 2,   // CPU_Implement.cpp:38-102 (fixed step)
+};
+
+// Per-pair arithmetic.
+enum Arith : int {
+    ARITH_FAST = 0,  // rsqrt + FMA, k applied once per vertex
+    ARITH_EXACT = 1, // the reference's IEEE operation sequence, bit-exact
+};
+
+// Charge record: pointCharge<T> of include/Electrostatics.h:30-35.
+struct alignas(32) ChargeD {
+    double x, y, z, q;
+};
+template <class T> struct ChargeRec;
+template <> struct ChargeRec<float> {
+    using type = float4;
+};
+template <> struct ChargeRec<double> {
+    using type = ChargeD;
+};
+
+// Parameters of the reference-layout tracer (CalcField_CPU semantics).
+template <class T> struct RefTraceParams {
+    T *x, *y, *z;              // n*total_steps each; vertex (line, s) at s*n + line
+    const void *charges;       // padded charge records, 16-B aligned
+    long long n;               // number of lines (row stride)
+    long long n_groups;        // ceil(n / lines_per_warp)
+    int total_steps;           // rows, including the seed row
+    int p_pad;                 // padded charge count (resident: all; streamed: n_tiles*tile)
+    int n_tiles;               // streamed: number of charge tiles
+    int tile_recs;             // streamed: records per tile
+    int stages;                // streamed: ring depth
+    int resident;              // 1: all charges staged once
+    int rule;                  // Rule
+    T resolution;
+    int *err;                  // device error word
+};
+
+struct LaunchCfg {
+    int tpl;     // threads per line (1, 2, 4, 8)
+    int warps;   // compute warps per CTA
+    int grid;    // CTAs
+    int resident;
+    int stages;
+    int tile_recs;
+    size_t smem; // dynamic shared memory bytes
+};
+
+// Charge padding granule per launch configuration (records).
+constexpr int kUnroll = 8;
+
+template <class T>
+cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
+                             cudaStream_t stream);
+
+// Writes the pad record {1e15, 1e15, 1e15, 0} into [first, last) of a
+// device charge array (its contribution is exactly zero in every mode).
+template <class T>
+cudaError_t launch_pad_charges(void *charges, int first, int last, cudaStream_t stream);
+
+// Adds k to the process-wide count of kernels launched by this library.
+void count_launch(unsigned long long k);
+
+// Field at m points, one thread per point (em_field.cu).
+template <class T>
+cudaError_t launch_field(const T *px, const T *py, const T *pz, long long m, const T *charges,
+                         int p, int arith, int three_arg, T *ex, T *ey, T *ez,
+                         cudaStream_t stream);
+
+} // namespace em

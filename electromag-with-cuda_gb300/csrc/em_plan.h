@@ -1,0 +1,145 @@
+// Per-device state and launch planning for the tracer kernels.
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <mutex>
+
+#include "em_internal.h"
+#include "emgb300.h"
+
+namespace em {
+
+constexpr int kMaxDevices = 64;
+
+// Cached per-device state.  `mu` serialises calls on one device; buffers
+// only grow and are released by em_release().
+struct DevCtx {
+    std::mutex init_mu, mu;
+    bool ready = false;
+    int device = 0;
+    int nsm = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void *charges = nullptr;
+    size_t charges_cap = 0;
+    void *lines = nullptr;
+    size_t lines_cap = 0;
+    void *errbuf = nullptr;
+    size_t errbuf_cap = 0;
+    void *scratch = nullptr; // field-at-points staging
+    size_t scratch_cap = 0;
+    int *err = nullptr;
+};
+
+DevCtx *get_ctx(int *code);
+int grow(void **buf, size_t *cap, size_t need);
+int map_cuda(cudaError_t e);
+int read_dev_err(DevCtx &c, cudaStream_t s, int *dev_err_host);
+
+struct Plan {
+    LaunchCfg cfg{};
+    long long n_groups = 0;
+    int p_pad = 0;
+    int n_tiles = 0;
+};
+
+inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
+
+// Relative cost of one line-group step for `tpl` threads per line: pair
+// work per lane plus the butterfly and the per-vertex step.
+inline double group_step_cost(long long p, int tpl)
+{
+    int lg = 0;
+    for (int t = tpl; t > 1; t >>= 1)
+        ++lg;
+    return (double)ceil_div(p, tpl) * 13.0 + 18.0 * lg + 120.0;
+}
+
+// Picks threads per line, compute warps per CTA and the grid for n lines
+// and p charges on a device with nsm SMs (one persistent CTA per SM).  The
+// model charges each SM sub-partition (4 per SM) for the warps it runs.
+inline void choose_shape(long long n, long long p, int nsm, int max_warps, int fixed_tpl,
+                         int *tpl_out, int *warps_out)
+{
+    double best = 0;
+    int bt = 1, bw = 1;
+    for (int tpl = 1; tpl <= 8; tpl <<= 1) {
+        if (fixed_tpl && tpl != fixed_tpl)
+            continue;
+        const long long lpw = 32 / tpl;
+        const long long groups = ceil_div(n, lpw);
+        const long long grid = std::min<long long>(nsm, groups);
+        const long long gpc = ceil_div(groups, grid);
+        const int warps = (int)std::min<long long>(max_warps, gpc);
+        const long long rounds = ceil_div(gpc, warps);
+        const long long last = gpc - (rounds - 1) * warps;
+        double per_smsp = (double)(rounds - 1) * (double)ceil_div(warps, 4) +
+                          (double)ceil_div(last, 4);
+        // one warp per sub-partition cannot hide the FP32 pipe latency
+        if (ceil_div(warps, 4) < 2)
+            per_smsp *= 1.6;
+        const double t = per_smsp * group_step_cost(p, tpl);
+        if (best == 0 || t < best * 0.98) {
+            best = t;
+            bt = tpl;
+            bw = warps;
+        }
+    }
+    *tpl_out = bt;
+    *warps_out = bw;
+}
+
+template <class T>
+int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl)
+{
+    const size_t rec = sizeof(T) * 4;
+    const int fixed_tpl = o.arith == EM_ARITH_EXACT ? 1 : o.threads_per_line;
+    if (fixed_tpl != 0 && fixed_tpl != 1 && fixed_tpl != 2 && fixed_tpl != 4 && fixed_tpl != 8)
+        return EM_ERR_ARG;
+    if (o.warps_per_cta < 0 || o.warps_per_cta > 32 || o.tile_charges < 0)
+        return EM_ERR_ARG;
+    const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
+    int tpl = 1, warps = 1;
+    // resident if the padded set fits next to the barrier block
+    const size_t gran_max = 8 * kUnroll;
+    const size_t p_res = (p + gran_max - 1) / gran_max * gran_max;
+    const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
+    choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, &tpl,
+                 &warps);
+    if (o.warps_per_cta)
+        warps = std::min(o.warps_per_cta, resident ? 32 : 31);
+    const int gran = tpl * kUnroll;
+    Plan r;
+    r.n_groups = ceil_div((long long)n, 32 / tpl);
+    r.cfg.tpl = tpl;
+    r.cfg.warps = warps;
+    r.cfg.grid = (int)std::min<long long>(c.nsm, r.n_groups);
+    r.cfg.resident = resident ? 1 : 0;
+    if (resident) {
+        r.p_pad = (int)((p + gran - 1) / gran * gran);
+        r.n_tiles = 1;
+        r.cfg.stages = 1;
+        r.cfg.tile_recs = r.p_pad;
+        r.cfg.smem = 128 + (size_t)r.p_pad * rec;
+    } else {
+        int tile = o.tile_charges ? o.tile_charges : (rec == 16 ? 1024 : 512);
+        tile = (tile + gran - 1) / gran * gran;
+        r.cfg.stages = 4;
+        while (r.cfg.stages > 2 && 128 + (size_t)r.cfg.stages * tile * rec > smem_cap)
+            --r.cfg.stages;
+        if (128 + (size_t)r.cfg.stages * tile * rec > smem_cap)
+            return EM_ERR_ARG;
+        r.n_tiles = (int)ceil_div((long long)p, tile);
+        if (r.n_tiles == 0)
+            r.n_tiles = 1;
+        r.p_pad = r.n_tiles * tile;
+        r.cfg.tile_recs = tile;
+        r.cfg.smem = 128 + (size_t)r.cfg.stages * tile * rec;
+    }
+    *pl = r;
+    return EM_OK;
+}
+
+} // namespace em

@@ -1,0 +1,366 @@
+// Field-line tracer over the reference's SoA line layout (CalcField_CPU
+// semantics, ElectroMag/src/CPU_Implement.cpp:38-527).
+//
+// Work decomposition.  A warp traces a group of 32/TPL lines for all steps;
+// TPL lanes share one line and split its charge sum (lane t takes charges
+// t, t+TPL, ...), combining the partial fields with an xor butterfly so every
+// lane of the line holds the same bits.  Groups are dealt to CTAs round-robin
+// (group g -> CTA g mod grid) so every SM gets the same number of lines.
+//
+// Charges live in shared memory.  If the padded set fits, one thread stages
+// it once with bulk (TMA) copies and the CTA never synchronises again.
+// Otherwise a producer warp streams fixed-size tiles through a ring of
+// `stages` buffers (full/empty mbarriers); all compute warps consume every
+// tile, idle warps only take part in the barrier protocol.
+//
+// Arithmetic.  ARITH_FAST: r2 by FMA, rsqrtf, s = q*inv^3, a += s*r; the
+// Coulomb constant is applied once per vertex.  ARITH_EXACT: the reference's
+// operation order with one IEEE rounding per operation (__f*_rn intrinsics,
+// no contraction), which reproduces the strict x86 build bit for bit.  The
+// per-vertex step (curvature, vec3SetInvLen, include/Vector.h:157-164) uses
+// the IEEE sequence in both modes.
+#include "em_device.cuh"
+#include "em_internal.h"
+
+namespace em {
+namespace {
+
+// ---- scalar IEEE operations without contraction --------------------------
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float sqrt_rn(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
+
+__device__ __forceinline__ float rsqrt_fast(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double rsqrt_fast(double a) { return rsqrt(a); }
+
+struct C4f {
+    float x, y, z, q;
+};
+struct C4d {
+    double x, y, z, q;
+};
+__device__ __forceinline__ C4f load_charge(const float4 *s, int j)
+{
+    const float4 c = s[j];
+    return {c.x, c.y, c.z, c.w};
+}
+__device__ __forceinline__ C4d load_charge(const ChargeD *s, int j)
+{
+    const double2 *p = reinterpret_cast<const double2 *>(s + j);
+    const double2 a = p[0], b = p[1];
+    return {a.x, a.y, b.x, b.y};
+}
+template <class T> struct C4;
+template <> struct C4<float> {
+    using type = C4f;
+};
+template <> struct C4<double> {
+    using type = C4d;
+};
+
+// One pair, fast form: a += q * r / |r|^3.
+template <class T, class C>
+__device__ __forceinline__ void pair_fast(T px, T py, T pz, const C &c, T &ax, T &ay, T &az)
+{
+    const T dx = px - c.x, dy = py - c.y, dz = pz - c.z;
+    const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+    const T inv = rsqrt_fast(r2);
+    const T s = (c.q * inv) * (inv * inv);
+    ax = fma(s, dx, ax);
+    ay = fma(s, dy, ay);
+    az = fma(s, dz, az);
+}
+
+// One pair, the reference's sequence.  three_arg: PartField(charge, point, k)
+// = r*k*q / (r2*sqrt(r2)) (include/Electrostatics.h:38-51, the SSE paths);
+// otherwise PartField(charge, point) = r * (k*q / (r2*sqrt(r2))) (:53-60).
+template <class T, class C>
+__device__ __forceinline__ void pair_exact(T px, T py, T pz, const C &c, T K, bool three_arg,
+                                           T &ax, T &ay, T &az)
+{
+    const T rx = sub_rn(px, c.x), ry = sub_rn(py, c.y), rz = sub_rn(pz, c.z);
+    const T l2 = add_rn(add_rn(mul_rn(rx, rx), mul_rn(ry, ry)), mul_rn(rz, rz));
+    const T d = mul_rn(l2, sqrt_rn(l2));
+    if (three_arg) {
+        ax = add_rn(ax, div_rn(mul_rn(mul_rn(rx, K), c.q), d));
+        ay = add_rn(ay, div_rn(mul_rn(mul_rn(ry, K), c.q), d));
+        az = add_rn(az, div_rn(mul_rn(mul_rn(rz, K), c.q), d));
+    } else {
+        const T s = div_rn(mul_rn(K, c.q), d);
+        ax = add_rn(ax, mul_rn(rx, s));
+        ay = add_rn(ay, mul_rn(ry, s));
+        az = add_rn(az, mul_rn(rz, s));
+    }
+}
+
+// Advance one vertex: the curvature rule of CPU_Implement.cpp:327-331
+// (r0 = curvature reference vector) or the fixed step of :89-90.
+template <class T>
+__device__ __forceinline__ void advance(T ex, T ey, T ez, T r0x, T r0y, T r0z, bool curvature,
+                                        T res, T &px, T &py, T &pz)
+{
+    const T k2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+    T scale = res;
+    if (curvature) {
+        const T ix = sub_rn(ex, r0x), iy = sub_rn(ey, r0y), iz = sub_rn(ez, r0z);
+        const T cx = sub_rn(mul_rn(iy, r0z), mul_rn(iz, r0y));
+        const T cy = sub_rn(mul_rn(iz, r0x), mul_rn(ix, r0z));
+        const T cz = sub_rn(mul_rn(ix, r0y), mul_rn(iy, r0x));
+        const T c2 = add_rn(add_rn(mul_rn(cx, cx), mul_rn(cy, cy)), mul_rn(cz, cz));
+        const T kc = div_rn(sqrt_rn(c2), mul_rn(k2, sqrt_rn(k2)));
+        scale = mul_rn(add_rn(kc, T(1)), res);
+    }
+    const T s = mul_rn(scale, sqrt_rn(k2));
+    px = add_rn(px, div_rn(ex, s));
+    py = add_rn(py, div_rn(ey, s));
+    pz = add_rn(pz, div_rn(ez, s));
+}
+
+// Sum of one line's charges held in shared memory [0, count), lane t of TPL.
+template <class T, int TPL, int ARITH, class Rec>
+__device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T px, T py, T pz,
+                                           T K, bool three_arg, T &ax, T &ay, T &az)
+{
+    if (ARITH == ARITH_FAST) {
+#pragma unroll kUnroll
+        for (int j = t; j < count; j += TPL)
+            pair_fast<T>(px, py, pz, load_charge(tile, j), ax, ay, az);
+    } else {
+#pragma unroll 2
+        for (int j = t; j < count; j += TPL)
+            pair_exact<T>(px, py, pz, load_charge(tile, j), K, three_arg, ax, ay, az);
+    }
+}
+
+template <class T, int TPL>
+__device__ __forceinline__ T line_reduce(T v)
+{
+#pragma unroll
+    for (int o = TPL / 2; o >= 1; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class T, int TPL, int ARITH>
+__global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams<T> P)
+{
+    using Rec = typename ChargeRec<T>::type;
+    constexpr int LPW = 32 / TPL;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    Rec *tiles = reinterpret_cast<Rec *>(smem + 128);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const bool streamed = !P.resident;
+    const int ncw = streamed ? nwarps - 1 : nwarps;
+    const int NST = streamed ? P.stages : 1;
+    if (NST > 8 || ncw < 1) {
+        if (threadIdx.x == 0)
+            atomicCAS(P.err, 0, EM_DEVERR_CONFIG);
+        return;
+    }
+    const uint32_t full0 = smem_addr(bars), empty0 = smem_addr(bars + 8);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, ncw);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    const long long cta_groups =
+        blockIdx.x < P.n_groups ? (P.n_groups - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const int rounds = (int)((cta_groups + ncw - 1) / ncw);
+    const T K = (T)kElectroK;
+    const bool curvature = P.rule != RULE_FIXED;
+    const bool three_arg = P.rule == RULE_SSE;
+    const int t = lane % TPL;
+    const size_t n = (size_t)P.n;
+
+    if (!streamed) {
+        if (threadIdx.x == 0) {
+            const uint32_t bytes = (uint32_t)P.p_pad * (uint32_t)sizeof(Rec);
+            mbar_arrive_expect_tx(full0, bytes);
+            const char *src = static_cast<const char *>(P.charges);
+            const uint32_t dst = smem_addr(tiles);
+            constexpr uint32_t CH = 32768;
+            for (uint32_t off = 0; off < bytes; off += CH)
+                bulk_g2s(dst + off, src + off, bytes - off < CH ? bytes - off : CH, full0);
+        }
+        if (!mbar_wait(full0, 0, P.err))
+            return;
+    }
+
+    if (streamed && warp == nwarps - 1) {
+        // ---- producer warp: one lane issues every tile copy -------------------
+        if (lane == 0) {
+            const uint32_t tb = (uint32_t)P.tile_recs * (uint32_t)sizeof(Rec);
+            const char *src = static_cast<const char *>(P.charges);
+            uint32_t it = 0;
+            bool ok = true;
+            for (int r = 0; r < rounds && ok; ++r)
+                for (int step = 1; step < P.total_steps && ok; ++step)
+                    for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+                        const uint32_t s = it % NST, ph = (it / NST) & 1;
+                        if (it >= (uint32_t)NST && !mbar_wait(empty0 + 8 * s, ph ^ 1, P.err)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(full0 + 8 * s, tb);
+                        bulk_g2s(smem_addr(tiles) + s * tb, src + (size_t)tile * tb, tb,
+                                 full0 + 8 * s);
+                    }
+            // Drain: the latest copy on each stage must have landed before
+            // the CTA may exit (bounded like every other wait).
+            const uint32_t last = it;
+            for (uint32_t k = 0; k < (uint32_t)NST && k < last; ++k) {
+                const uint32_t j = last - 1 - k;
+                mbar_wait(full0 + 8 * (j % NST), (j / NST) & 1, P.err);
+            }
+        }
+        return;
+    }
+
+    // ---- compute warps --------------------------------------------------------
+    uint32_t it = 0;
+    for (int r = 0; r < rounds; ++r) {
+        const long long k = (long long)r * ncw + warp;
+        const long long g = blockIdx.x + (long long)gridDim.x * k;
+        const bool active = k < cta_groups;
+        const long long line = g * LPW + lane / TPL;
+        const bool own = active && line < P.n;
+        T px = 0, py = 0, pz = 0;
+        if (own) {
+            px = P.x[line];
+            py = P.y[line];
+            pz = P.z[line];
+        }
+        // SSE rule: the curvature vector is the seed, loaded once
+        // (CPU_Implement.cpp:254-256) and never updated.
+        T r0x = px, r0y = py, r0z = pz;
+        if (!streamed && !active)
+            break;
+        for (int step = 1; step < P.total_steps; ++step) {
+            T ax = 0, ay = 0, az = 0;
+            if (!streamed) {
+                accumulate<T, TPL, ARITH>(tiles, P.p_pad, t, px, py, pz, K, three_arg, ax, ay,
+                                          az);
+            } else {
+                for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+                    const uint32_t s = it % NST, ph = (it / NST) & 1;
+                    if (!mbar_wait(full0 + 8 * s, ph, P.err))
+                        return;
+                    if (active)
+                        accumulate<T, TPL, ARITH>(tiles + s * P.tile_recs, P.tile_recs, t, px,
+                                                  py, pz, K, three_arg, ax, ay, az);
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(empty0 + 8 * s);
+                }
+                if (!active)
+                    continue;
+            }
+            if (TPL > 1) {
+                ax = line_reduce<T, TPL>(ax);
+                ay = line_reduce<T, TPL>(ay);
+                az = line_reduce<T, TPL>(az);
+            }
+            if (ARITH == ARITH_FAST) {
+                ax = mul_rn(ax, K);
+                ay = mul_rn(ay, K);
+                az = mul_rn(az, K);
+            }
+            if (P.rule == RULE_GENERIC) {
+                // prevVec = previous point (CPU_Implement.cpp:148-153)
+                r0x = px;
+                r0y = py;
+                r0z = pz;
+            }
+            advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px, py, pz);
+            if (own && t == 0) {
+                const size_t idx = (size_t)step * n + (size_t)line;
+                store_stream(P.x + idx, px);
+                store_stream(P.y + idx, py);
+                store_stream(P.z + idx, pz);
+            }
+        }
+    }
+}
+
+template <class T>
+__global__ void pad_kernel(typename ChargeRec<T>::type *c, int first, int last)
+{
+    const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < last) {
+        typename C4<T>::type v{T(1e15), T(1e15), T(1e15), T(0)};
+        T *d = reinterpret_cast<T *>(c + i);
+        d[0] = v.x;
+        d[1] = v.y;
+        d[2] = v.z;
+        d[3] = v.q;
+    }
+}
+
+template <class T, int TPL, int ARITH>
+cudaError_t launch_one(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
+{
+    auto kern = ref_trace_kernel<T, TPL, ARITH>;
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess)
+        return e;
+    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
+    kern<<<cfg.grid, threads, cfg.smem, stream>>>(p);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+template <class T>
+cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
+                             cudaStream_t stream)
+{
+    if (arith == ARITH_EXACT) {
+        if (cfg.tpl != 1)
+            return cudaErrorInvalidValue;
+        return launch_one<T, 1, ARITH_EXACT>(p, cfg, stream);
+    }
+    switch (cfg.tpl) {
+    case 1: return launch_one<T, 1, ARITH_FAST>(p, cfg, stream);
+    case 2: return launch_one<T, 2, ARITH_FAST>(p, cfg, stream);
+    case 4: return launch_one<T, 4, ARITH_FAST>(p, cfg, stream);
+    case 8: return launch_one<T, 8, ARITH_FAST>(p, cfg, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <class T>
+cudaError_t launch_pad_charges(void *charges, int first, int last, cudaStream_t stream)
+{
+    if (last <= first)
+        return cudaSuccess;
+    const int cnt = last - first;
+    pad_kernel<T><<<(cnt + 127) / 128, 128, 0, stream>>>(
+        static_cast<typename ChargeRec<T>::type *>(charges), first, last);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_ref_trace<float>(const RefTraceParams<float> &, const LaunchCfg &,
+                                             int, cudaStream_t);
+template cudaError_t launch_ref_trace<double>(const RefTraceParams<double> &,
+                                              const LaunchCfg &, int, cudaStream_t);
+template cudaError_t launch_pad_charges<float>(void *, int, int, cudaStream_t);
+template cudaError_t launch_pad_charges<double>(void *, int, int, cudaStream_t);
+
+} // namespace em

@@ -1,0 +1,149 @@
+/*
+ * emgb300.h — C ABI of the GB300 field-line tracer (libemgb300.so).
+ *
+ * Drop-in for ElectroMag's calc-field entry points:
+ *   int CalcField_CPU<T>(Vector3<Array<T>>& fieldLines,
+ *                        Array<pointCharge<T>>& pointCharges, size_t n,
+ *                        T resolution, perfPacket& perfData,
+ *                        bool useCurvature)
+ *       ElectroMag/src/"CPU Implement.h":25-30, CPU_Implement.cpp:501-527
+ *   int CalcField(Array<Vector3<T>>&, Array<pointCharge<T>>&, size_t n,
+ *                 T resolution, perfPacket&, bool useCurvature)
+ *       GPGPU_Segment/src/Electrostatics.cpp:28-42 (stubs returning -1)
+ *
+ * Layout contract (the reference's, include/SOA_utils.hpp:31-112):
+ *   field lines  three component arrays x, y, z of n*total_steps elements;
+ *                vertex (line, step) at index step*n + line; row 0 holds
+ *                the seeds, rows 1..total_steps-1 are written.
+ *   charges      p records {x, y, z, q} of the element type (16 B for
+ *                float, 32 B for double; pointCharge<T>,
+ *                include/Electrostatics.h:30-35), 16-B aligned.
+ * The caller owns every buffer.  Calls are synchronous unless a stream is
+ * given through em_options with device pointers.  No call aborts: every
+ * failure is a return code.
+ */
+#ifndef EMGB300_H
+#define EMGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define EM_API __attribute__((visibility("default")))
+#else
+#define EM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes -------------------------------------------------------
+ * 0..5 are the reference's (CPU_Implement.cpp:213-230); the rest are new. */
+#define EM_OK 0
+#define EM_ERR_N_ZERO 1        /* n == 0                                  */
+#define EM_ERR_RESOLUTION 2    /* resolution == 0                         */
+#define EM_ERR_STEPS 3         /* total_steps < 2                         */
+#define EM_ERR_ARG 4           /* null pointer, misaligned or bad option  */
+#define EM_ERR_N_ALIGN 5       /* n % 64 != 0 while reproducing the SSE
+                                  path's restriction (CPU_Implement.cpp:223) */
+#define EM_ERR_CUDA 10         /* a CUDA runtime call failed               */
+#define EM_ERR_NOMEM 11        /* device allocation failed                 */
+#define EM_ERR_TIMEOUT 12      /* a device-side wait hit its time limit    */
+#define EM_ERR_NO_DEVICE 13    /* no CUDA device / library not usable      */
+#define EM_ERR_TOO_LARGE 14    /* sizes beyond what the entry point takes  */
+
+/* ---- arithmetic of the pair sum ------------------------------------------ */
+#define EM_ARITH_FAST 0   /* FP32 (or FP64 for _f64) rsqrt + FMA             */
+#define EM_ARITH_EXACT 1  /* the reference's IEEE operation sequence:
+                             bit-identical to its strict x86 build          */
+
+/* ---- stepping rule (which reference routine to reproduce) ---------------- */
+#define EM_RULE_SSE 0      /* CalcField_CPU_T_Curvature<float/double> SSE
+                              specialisations, CPU_Implement.cpp:207-498: the
+                              curvature vector is the line's seed           */
+#define EM_RULE_GENERIC 1  /* the generic template, CPU_Implement.cpp:104-191
+                              (non-SSE builds): previous point              */
+
+/* Performance record; the fields of perfPacket ("Data Structures.h":221-236)
+ * plus the work counted by this library. */
+typedef struct em_perf {
+    double performance;  /* GFLOP/s, reference accounting:
+                            n*(steps-1)*(18*p+13)/time (CPU_Implement.cpp:348) */
+    double time;         /* seconds of device execution (CUDA events)        */
+    volatile double progress; /* 0 before the call, 1.0 when complete        */
+    double pairs;        /* pair interactions evaluated                      */
+    double wall_time;    /* seconds of the whole call (copies included)      */
+} em_perf;
+
+/* Options for the _ex entry points.  Zero-initialise and set what you need. */
+typedef struct em_options {
+    int arith;        /* EM_ARITH_*                                          */
+    int rule;         /* EM_RULE_* (curvature runs only)                     */
+    int require_n64;  /* 1: return EM_ERR_N_ALIGN for n % 64 like the SSE
+                         path; 0: any n                                      */
+    int device_ptrs;  /* 1: x, y, z and charges are device pointers          */
+    void *stream;     /* cudaStream_t for device_ptrs calls (NULL: the
+                         library's stream, call returns when done)           */
+    int threads_per_line; /* 0: automatic; else 1, 2, 4 or 8                 */
+    int warps_per_cta;    /* 0: automatic; else 1..32                        */
+    int tile_charges;     /* 0: automatic; streamed-charge tile size         */
+    int force_streamed;   /* 1: stream charge tiles even if they fit          */
+} em_options;
+
+/* Reference-compatible entry points (host pointers, synchronous).
+ * Replace CalcField_CPU<float>/<double> (CPU_Implement.cpp:501-527): same
+ * layout, same codes in the same order (n == 0 -> 1, resolution == 0 -> 2,
+ * curvature with n % 64 -> 5, total_steps < 2 -> 3).  total_steps is the
+ * reference's fieldLines.GetSize()/n (CPU_Implement.cpp:219). */
+EM_API int em_calc_field_f32(float *x, float *y, float *z, size_t n, size_t total_steps,
+                      const float *charges, size_t p, float resolution,
+                      int use_curvature, em_perf *perf);
+EM_API int em_calc_field_f64(double *x, double *y, double *z, size_t n,
+                      size_t total_steps, const double *charges, size_t p,
+                      double resolution, int use_curvature, em_perf *perf);
+
+/* The same with options: device pointers, streams, arithmetic, stepping
+ * rule, the n % 64 restriction lifted (require_n64 = 0). */
+EM_API int em_calc_field_ex_f32(float *x, float *y, float *z, size_t n,
+                         size_t total_steps, const float *charges, size_t p,
+                         float resolution, int use_curvature,
+                         const em_options *opt, em_perf *perf);
+EM_API int em_calc_field_ex_f64(double *x, double *y, double *z, size_t n,
+                         size_t total_steps, const double *charges, size_t p,
+                         double resolution, int use_curvature,
+                         const em_options *opt, em_perf *perf);
+
+/* Field at m points, no stepping: E_i = sum_j PartField(charge_j, point_i)
+ * summed in charge order (include/Electrostatics.h:38-60 as
+ * CPU_Implement.cpp:274-320 sums it).  Points are SoA px/py/pz; the result
+ * goes to ex/ey/ez.  Host pointers unless opt->device_ptrs.  With
+ * EM_ARITH_EXACT, opt->rule picks the PartField form: EM_RULE_SSE the
+ * three-argument one (:38-51), EM_RULE_GENERIC the two-argument one (:53-60).
+ * opt may be NULL (fast arithmetic, host pointers). */
+EM_API int em_field_f32(const float *px, const float *py, const float *pz,
+                        size_t m, const float *charges, size_t p, float *ex,
+                        float *ey, float *ez, const em_options *opt);
+EM_API int em_field_f64(const double *px, const double *py, const double *pz,
+                        size_t m, const double *charges, size_t p, double *ex,
+                        double *ey, double *ez, const em_options *opt);
+
+/* Library state.  em_device_count: CUDA devices visible (0 when none).
+ * em_release: frees the cached device buffers of the current device.
+ * em_strerror: text for a return code. */
+EM_API int em_device_count(void);
+EM_API int em_release(void);
+EM_API const char *em_strerror(int code);
+/* Diagnostics.  em_fp32_peak_tflops: measured FP32 FFMA throughput of the
+ * current device (dense FMA chains, 2 FLOP per FMA), the denominator of the
+ * tracer's FP32 roofline.  em_launch_count: kernels this library has
+ * launched in this process. */
+EM_API int em_fp32_peak_tflops(double *tflops, double *seconds);
+EM_API unsigned long long em_launch_count(void);
+/* Library version, "major.minor.patch". */
+EM_API const char *em_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EMGB300_H */

@@ -1,0 +1,111 @@
+"""TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT.
+
+ctypes wrapper of liboracle.so (oracle/em_oracle.c), the CPU restatement of
+the reference tracer.  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg import this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+CURV_SSE, CURV_GENERIC, FIXED = 0, 1, 2
+TERM_STEPS, TERM_CHARGE, TERM_NULL = 0, 1, 2
+
+P, S, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+_lib = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = ctypes.CDLL(LIB)
+        lib.orc_calc_field_f32.argtypes = [P, P, P, S, S, P, S, ctypes.c_float,
+                                           I, S, S, I]
+        lib.orc_calc_field_f64.argtypes = [P, P, P, S, S, P, S, ctypes.c_double,
+                                           I, S, S, I]
+        lib.orc_field_f32.argtypes = [P, P, P, S, P, S, I, P, P, P]
+        lib.orc_field_f64.argtypes = [P, P, P, S, P, S, P, P, P, P, I]
+        lib.orc_trace_lines_f64.argtypes = [P, S, P, P, P, S, S, P,
+                                            ctypes.c_double, ctypes.c_double,
+                                            P, P, I]
+        lib.orc_seed_fibonacci_f64.argtypes = [P, S, S, ctypes.c_double, P, P,
+                                               P, S]
+        lib.orc_seed_fibonacci_f64.restype = S
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+def calc_field(x, y, z, charges, n, resolution=1.0, variant=CURV_SSE,
+               line0=0, nlines=0, nthreads=0):
+    """Runs the restatement in place on the reference layout; returns rc."""
+    lib = load()
+    f32 = x.dtype == np.float32
+    ch = np.ascontiguousarray(charges, x.dtype)
+    fn = lib.orc_calc_field_f32 if f32 else lib.orc_calc_field_f64
+    steps = x.size // n if n else 0
+    return fn(_p(x), _p(y), _p(z), n, steps, _p(ch), ch.size // 4,
+              resolution, variant, line0, nlines, nthreads)
+
+
+def field_f64(points, charges, nthreads=0, with_maxc=False):
+    """FP64 field at points (m,3) from charges (p,4); optionally the largest
+    single contribution per point."""
+    lib = load()
+    pts = np.ascontiguousarray(np.asarray(points, np.float64).T)
+    ch = np.ascontiguousarray(charges, np.float64)
+    m = pts.shape[1]
+    e = np.zeros((3, m))
+    mc = np.zeros(m) if with_maxc else None
+    lib.orc_field_f64(_p(pts[0]), _p(pts[1]), _p(pts[2]), m, _p(ch),
+                      ch.size // 4, _p(e[0]), _p(e[1]), _p(e[2]), _p(mc),
+                      nthreads)
+    return (e.T, mc) if with_maxc else e.T
+
+
+def field_f32(points, charges, three_arg=True):
+    lib = load()
+    pts = np.ascontiguousarray(np.asarray(points, np.float32).T)
+    ch = np.ascontiguousarray(charges, np.float32)
+    m = pts.shape[1]
+    e = np.zeros((3, m), np.float32)
+    lib.orc_field_f32(_p(pts[0]), _p(pts[1]), _p(pts[2]), m, _p(ch),
+                      ch.size // 4, int(three_arg), _p(e[0]), _p(e[1]),
+                      _p(e[2]))
+    return e.T
+
+
+def trace_lines_f64(charges, seeds, max_steps, resolution=1.0,
+                    term_radius=0.5, max_steps_per_line=None, nthreads=0):
+    """Extended method in FP64; returns (vertices (3, max_steps, n), len, cls)."""
+    lib = load()
+    ch = np.ascontiguousarray(charges, np.float64)
+    seeds = np.asarray(seeds, np.float64)
+    n = len(seeds)
+    v = np.full((3, max_steps, n), np.nan)
+    v[:, 0, :] = seeds.T
+    ln = np.zeros(n, np.int32)
+    cl = np.zeros(n, np.int32)
+    msl = None
+    if max_steps_per_line is not None:
+        msl = np.ascontiguousarray(max_steps_per_line, np.int32)
+    rc = lib.orc_trace_lines_f64(_p(ch), ch.size // 4, _p(v[0]), _p(v[1]),
+                                 _p(v[2]), n, max_steps, _p(msl), resolution,
+                                 term_radius, _p(ln), _p(cl), nthreads)
+    if rc:
+        raise RuntimeError(f"orc_trace_lines_f64 returned {rc}")
+    return v, ln, cl
