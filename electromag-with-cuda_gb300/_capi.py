@@ -31,6 +31,9 @@ EM_ERR_TOO_LARGE = 14
 
 EM_ARITH_FAST = 0
 EM_ARITH_EXACT = 1
+EM_PACK_AUTO = 0
+EM_PACK_SCALAR = 1
+EM_PACK_PAIRS = 2
 EM_RULE_SSE = 0
 EM_RULE_GENERIC = 1
 
@@ -45,7 +48,7 @@ class EmOptions(ctypes.Structure):
     _fields_ = [("arith", I), ("rule", I), ("require_n64", I),
                 ("device_ptrs", I), ("stream", P), ("threads_per_line", I),
                 ("warps_per_cta", I), ("tile_charges", I),
-                ("force_streamed", I)]
+                ("force_streamed", I), ("pack", I)]
 
 
 _SIGNATURES = {

@@ -140,6 +140,8 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
 
     if ((code = grow(&c.charges, &c.charges_cap, (size_t)pl.p_pad * rec)))
         return code;
+    if ((code = grow(&c.charges_raw, &c.charges_raw_cap, (size_t)p * rec + 16)))
+        return code;
     if ((code = grow(&c.errbuf, &c.errbuf_cap, 256)))
         return code;
     c.err = static_cast<int *>(c.errbuf);
@@ -156,9 +158,10 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     cudaError_t e = cudaSuccess;
     const cudaMemcpyKind kin = o.device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (p)
-        e = cudaMemcpyAsync(c.charges, charges, p * rec, kin, s);
+        e = cudaMemcpyAsync(c.charges_raw, charges, p * rec, kin, s);
     if (e == cudaSuccess)
-        e = launch_pad_charges<T>(c.charges, (int)p, pl.p_pad, s);
+        e = launch_stage_charges<T>(c.charges_raw, (int)p, c.charges, pl.p_pad,
+                                    pl.arith == ARITH_FAST2, s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(c.err, 0, sizeof(int), s);
     if (e == cudaSuccess && !o.device_ptrs) {
@@ -190,7 +193,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
 
     e = cudaEventRecord(c.ev0, s);
     if (e == cudaSuccess)
-        e = launch_ref_trace<T>(prm, pl.cfg, o.arith, s);
+        e = launch_ref_trace<T>(prm, pl.cfg, pl.arith, s);
     if (e == cudaSuccess)
         e = cudaEventRecord(c.ev1, s);
     if (e != cudaSuccess)
@@ -353,6 +356,7 @@ int em_release(void)
         return code;
     std::lock_guard<std::mutex> g(c->mu);
     for (auto pr : {std::make_pair(&c->charges, &c->charges_cap),
+                    std::make_pair(&c->charges_raw, &c->charges_raw_cap),
                     std::make_pair(&c->lines, &c->lines_cap),
                     std::make_pair(&c->scratch, &c->scratch_cap),
                     std::make_pair(&c->errbuf, &c->errbuf_cap)}) {

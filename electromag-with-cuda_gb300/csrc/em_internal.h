@@ -25,6 +25,7 @@ enum Rule : int {
 enum Arith : int {
     ARITH_FAST = 0,  // rsqrt + FMA, k applied once per vertex
     ARITH_EXACT = 1, // the reference's IEEE operation sequence, bit-exact
+    ARITH_FAST2 = 2, // fast form on packed FP32 pairs (.f32x2), paired charge layout
 };
 
 // Charge record: pointCharge<T> of include/Electrostatics.h:30-35.
@@ -73,10 +74,11 @@ template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream);
 
-// Writes the pad record {1e15, 1e15, 1e15, 0} into [first, last) of a
-// device charge array (its contribution is exactly zero in every mode).
+// Stages p raw charge records into p_pad records (pad record {1e15, 1e15,
+// 1e15, 0}, whose contribution is exactly zero), plain or pair-interleaved.
 template <class T>
-cudaError_t launch_pad_charges(void *charges, int first, int last, cudaStream_t stream);
+cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad, int paired,
+                                 cudaStream_t stream);
 
 // Adds k to the process-wide count of kernels launched by this library.
 void count_launch(unsigned long long k);

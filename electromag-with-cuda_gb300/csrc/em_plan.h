@@ -22,8 +22,10 @@ struct DevCtx {
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    void *charges = nullptr;
+    void *charges = nullptr; // staged (padded, possibly paired) charges
     size_t charges_cap = 0;
+    void *charges_raw = nullptr; // the caller's records, copied as given
+    size_t charges_raw_cap = 0;
     void *lines = nullptr;
     size_t lines_cap = 0;
     void *errbuf = nullptr;
@@ -40,6 +42,7 @@ int read_dev_err(DevCtx &c, cudaStream_t s, int *dev_err_host);
 
 struct Plan {
     LaunchCfg cfg{};
+    int arith = ARITH_FAST; // resolved kernel arithmetic (Arith)
     long long n_groups = 0;
     int p_pad = 0;
     int n_tiles = 0;
@@ -100,18 +103,25 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
         return EM_ERR_ARG;
     if (o.warps_per_cta < 0 || o.warps_per_cta > 32 || o.tile_charges < 0)
         return EM_ERR_ARG;
+    if (o.pack < EM_PACK_AUTO || o.pack > EM_PACK_PAIRS)
+        return EM_ERR_ARG;
+    int arith = o.arith == EM_ARITH_EXACT ? ARITH_EXACT : ARITH_FAST;
+    if (arith == ARITH_FAST && sizeof(T) == 4 && o.pack != EM_PACK_SCALAR)
+        arith = ARITH_FAST2;
     const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
     int tpl = 1, warps = 1;
     // resident if the padded set fits next to the barrier block
-    const size_t gran_max = 8 * kUnroll;
+    const size_t gran_max = 16 * kUnroll;
     const size_t p_res = (p + gran_max - 1) / gran_max * gran_max;
     const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
     choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, &tpl,
                  &warps);
     if (o.warps_per_cta)
         warps = std::min(o.warps_per_cta, resident ? 32 : 31);
-    const int gran = tpl * kUnroll;
+    // records per padding granule: every lane gets whole unrolled groups
+    const int gran = tpl * kUnroll * (arith == ARITH_FAST2 ? 2 : 1);
     Plan r;
+    r.arith = arith;
     r.n_groups = ceil_div((long long)n, 32 / tpl);
     r.cfg.tpl = tpl;
     r.cfg.warps = warps;

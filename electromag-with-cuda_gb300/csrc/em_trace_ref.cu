@@ -37,8 +37,70 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
 
-__device__ __forceinline__ float rsqrt_fast(float a) { return rsqrtf(a); }
+// MUFU reciprocal square root without the denormal-input fix-up sequence:
+// r2 is a sum of squares of coordinate differences and never denormal
+// unless the point sits on a charge, where both forms give inf.
+__device__ __forceinline__ float rsqrt_fast(float a)
+{
+    float d;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(d) : "f"(a));
+    return d;
+}
 __device__ __forceinline__ double rsqrt_fast(double a) { return rsqrt(a); }
+
+// ---- packed FP32 pairs (sm_100+ .f32x2): two charges per instruction ------
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 f2_sub(u64 a, u64 b)
+{
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 f2_mul(u64 a, u64 b)
+{
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 f2_fma(u64 a, u64 b, u64 c)
+{
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ u64 f2_pack(float lo, float hi)
+{
+    u64 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(u64 v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ u64 f2_rsqrt(u64 a)
+{
+    float lo, hi;
+    f2_unpack(a, lo, hi);
+    return f2_pack(rsqrt_fast(lo), rsqrt_fast(hi));
+}
+
+// Charge pair jp of a paired-layout tile {xa,xb,ya,yb,za,zb,qa,qb}:
+// a += q r / |r|^3 for both charges, lanes of the packed accumulators.
+__device__ __forceinline__ void pair2_fast(u64 px, u64 py, u64 pz, const ulonglong2 *tile,
+                                           int jp, u64 &ax, u64 &ay, u64 &az)
+{
+    const ulonglong2 A = tile[2 * jp], B = tile[2 * jp + 1];
+    const u64 dx = f2_sub(px, A.x), dy = f2_sub(py, A.y), dz = f2_sub(pz, B.x);
+    u64 r2 = f2_mul(dx, dx);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dz, dz, r2);
+    const u64 inv = f2_rsqrt(r2);
+    const u64 s = f2_mul(f2_mul(B.y, inv), f2_mul(inv, inv));
+    ax = f2_fma(s, dx, ax);
+    ay = f2_fma(s, dy, ay);
+    az = f2_fma(s, dz, az);
+}
 
 struct C4f {
     float x, y, z, q;
@@ -123,19 +185,48 @@ __device__ __forceinline__ void advance(T ex, T ey, T ez, T r0x, T r0y, T r0z, b
     pz = add_rn(pz, div_rn(ez, s));
 }
 
-// Sum of one line's charges held in shared memory [0, count), lane t of TPL.
+// Per-line field accumulator: scalar components, plus packed pairs for the
+// .f32x2 path (kept across charge tiles so tiling never changes the sum).
+template <class T> struct Acc {
+    T x = 0, y = 0, z = 0;
+    u64 X = 0, Y = 0, Z = 0;
+};
+
+// Adds the charges held in shared memory [0, count) to lane t's partial sum.
 template <class T, int TPL, int ARITH, class Rec>
 __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T px, T py, T pz,
-                                           T K, bool three_arg, T &ax, T &ay, T &az)
+                                           T K, bool three_arg, Acc<T> &a)
 {
-    if (ARITH == ARITH_FAST) {
+    if (ARITH == ARITH_FAST2) {
+        // charge pairs t, t+TPL, ... ; count is a multiple of 2*TPL
+        const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(tile);
+        const u64 PX = f2_pack(px, px), PY = f2_pack(py, py), PZ = f2_pack(pz, pz);
+#pragma unroll 4
+        for (int jp = t; jp < count / 2; jp += TPL)
+            pair2_fast(PX, PY, PZ, tp, jp, a.X, a.Y, a.Z);
+    } else if (ARITH == ARITH_FAST) {
 #pragma unroll kUnroll
         for (int j = t; j < count; j += TPL)
-            pair_fast<T>(px, py, pz, load_charge(tile, j), ax, ay, az);
+            pair_fast<T>(px, py, pz, load_charge(tile, j), a.x, a.y, a.z);
     } else {
 #pragma unroll 2
         for (int j = t; j < count; j += TPL)
-            pair_exact<T>(px, py, pz, load_charge(tile, j), K, three_arg, ax, ay, az);
+            pair_exact<T>(px, py, pz, load_charge(tile, j), K, three_arg, a.x, a.y, a.z);
+    }
+}
+
+// Folds the packed halves into the scalar components (packed path only).
+template <class T, int ARITH>
+__device__ __forceinline__ void acc_finish(Acc<T> &a)
+{
+    if (ARITH == ARITH_FAST2) {
+        float l, h;
+        f2_unpack(a.X, l, h);
+        a.x = l + h;
+        f2_unpack(a.Y, l, h);
+        a.y = l + h;
+        f2_unpack(a.Z, l, h);
+        a.z = l + h;
     }
 }
 
@@ -250,10 +341,9 @@ __global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams
         if (!streamed && !active)
             break;
         for (int step = 1; step < P.total_steps; ++step) {
-            T ax = 0, ay = 0, az = 0;
+            Acc<T> acc;
             if (!streamed) {
-                accumulate<T, TPL, ARITH>(tiles, P.p_pad, t, px, py, pz, K, three_arg, ax, ay,
-                                          az);
+                accumulate<T, TPL, ARITH>(tiles, P.p_pad, t, px, py, pz, K, three_arg, acc);
             } else {
                 for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
                     const uint32_t s = it % NST, ph = (it / NST) & 1;
@@ -261,7 +351,7 @@ __global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams
                         return;
                     if (active)
                         accumulate<T, TPL, ARITH>(tiles + s * P.tile_recs, P.tile_recs, t, px,
-                                                  py, pz, K, three_arg, ax, ay, az);
+                                                  py, pz, K, three_arg, acc);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(empty0 + 8 * s);
@@ -269,12 +359,14 @@ __global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams
                 if (!active)
                     continue;
             }
+            acc_finish<T, ARITH>(acc);
+            T ax = acc.x, ay = acc.y, az = acc.z;
             if (TPL > 1) {
                 ax = line_reduce<T, TPL>(ax);
                 ay = line_reduce<T, TPL>(ay);
                 az = line_reduce<T, TPL>(az);
             }
-            if (ARITH == ARITH_FAST) {
+            if (ARITH != ARITH_EXACT) {
                 ax = mul_rn(ax, K);
                 ay = mul_rn(ay, K);
                 az = mul_rn(az, K);
@@ -296,17 +388,32 @@ __global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams
     }
 }
 
+// Copies p charge records into the staged buffer of p_pad records, filling
+// [p, p_pad) with the pad record {1e15, 1e15, 1e15, 0} (its contribution is
+// exactly zero in every arithmetic), in plain {x,y,z,q} order or, when
+// `paired`, as pair-interleaved {xa,xb,ya,yb,za,zb,qa,qb} blocks.
 template <class T>
-__global__ void pad_kernel(typename ChargeRec<T>::type *c, int first, int last)
+__global__ void stage_kernel(const T *raw, int p, T *staged, int p_pad, int paired)
 {
-    const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < last) {
-        typename C4<T>::type v{T(1e15), T(1e15), T(1e15), T(0)};
-        T *d = reinterpret_cast<T *>(c + i);
-        d[0] = v.x;
-        d[1] = v.y;
-        d[2] = v.z;
-        d[3] = v.q;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p_pad)
+        return;
+    T v[4];
+    if (i < p) {
+        for (int c = 0; c < 4; ++c)
+            v[c] = raw[4 * (size_t)i + c];
+    } else {
+        v[0] = v[1] = v[2] = T(1e15);
+        v[3] = T(0);
+    }
+    if (!paired) {
+        for (int c = 0; c < 4; ++c)
+            staged[4 * (size_t)i + c] = v[c];
+    } else {
+        const size_t base = 8 * (size_t)(i >> 1);
+        const int h = i & 1;
+        for (int c = 0; c < 4; ++c)
+            staged[base + 2 * c + h] = v[c];
     }
 }
 
@@ -335,6 +442,17 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, i
             return cudaErrorInvalidValue;
         return launch_one<T, 1, ARITH_EXACT>(p, cfg, stream);
     }
+    if (arith == ARITH_FAST2) {
+        if (sizeof(T) != 4)
+            return cudaErrorInvalidValue;
+        switch (cfg.tpl) {
+        case 1: return launch_one<T, 1, ARITH_FAST2>(p, cfg, stream);
+        case 2: return launch_one<T, 2, ARITH_FAST2>(p, cfg, stream);
+        case 4: return launch_one<T, 4, ARITH_FAST2>(p, cfg, stream);
+        case 8: return launch_one<T, 8, ARITH_FAST2>(p, cfg, stream);
+        default: return cudaErrorInvalidValue;
+        }
+    }
     switch (cfg.tpl) {
     case 1: return launch_one<T, 1, ARITH_FAST>(p, cfg, stream);
     case 2: return launch_one<T, 2, ARITH_FAST>(p, cfg, stream);
@@ -345,13 +463,13 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, i
 }
 
 template <class T>
-cudaError_t launch_pad_charges(void *charges, int first, int last, cudaStream_t stream)
+cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad, int paired,
+                                 cudaStream_t stream)
 {
-    if (last <= first)
+    if (p_pad <= 0)
         return cudaSuccess;
-    const int cnt = last - first;
-    pad_kernel<T><<<(cnt + 127) / 128, 128, 0, stream>>>(
-        static_cast<typename ChargeRec<T>::type *>(charges), first, last);
+    stage_kernel<T><<<(p_pad + 127) / 128, 128, 0, stream>>>(
+        static_cast<const T *>(raw), p, static_cast<T *>(staged), p_pad, paired);
     count_launch(1);
     return cudaGetLastError();
 }
@@ -360,7 +478,9 @@ template cudaError_t launch_ref_trace<float>(const RefTraceParams<float> &, cons
                                              int, cudaStream_t);
 template cudaError_t launch_ref_trace<double>(const RefTraceParams<double> &,
                                               const LaunchCfg &, int, cudaStream_t);
-template cudaError_t launch_pad_charges<float>(void *, int, int, cudaStream_t);
-template cudaError_t launch_pad_charges<double>(void *, int, int, cudaStream_t);
+template cudaError_t launch_stage_charges<float>(const void *, int, void *, int, int,
+                                                 cudaStream_t);
+template cudaError_t launch_stage_charges<double>(const void *, int, void *, int, int,
+                                                  cudaStream_t);
 
 } // namespace em

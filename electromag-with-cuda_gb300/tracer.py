@@ -15,6 +15,8 @@ from . import _capi
 
 _ARITH = {"fast": _capi.EM_ARITH_FAST, "exact": _capi.EM_ARITH_EXACT}
 _RULE = {"sse": _capi.EM_RULE_SSE, "generic": _capi.EM_RULE_GENERIC}
+_PACK = {"auto": _capi.EM_PACK_AUTO, "scalar": _capi.EM_PACK_SCALAR,
+         "pairs": _capi.EM_PACK_PAIRS}
 
 
 def _is_torch(a):
@@ -43,7 +45,7 @@ def _check(a, dtype_name):
 def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                arith="fast", rule="sse", require_n64=None, stream=None,
                threads_per_line=0, warps_per_cta=0, tile_charges=0,
-               force_streamed=False, plain=None):
+               force_streamed=False, pack="auto", plain=None):
     """Traces n field lines in place; returns (rc, perf).
 
     rc is the reference's code (0 ok, 1 n == 0, 2 resolution == 0,
@@ -65,7 +67,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
         plain = (not device and arith == "fast" and rule == "sse"
                  and require_n64 in (None, True) and not threads_per_line
                  and not warps_per_cta and not tile_charges
-                 and not force_streamed)
+                 and not force_streamed and pack == "auto")
     if plain:
         if device:
             raise ValueError("the plain entry point takes host arrays")
@@ -87,6 +89,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     o.warps_per_cta = warps_per_cta
     o.tile_charges = tile_charges
     o.force_streamed = int(bool(force_streamed))
+    o.pack = _PACK[pack]
     fn = lib.em_calc_field_ex_f32 if f32 else lib.em_calc_field_ex_f64
     rc = fn(_ptr(x), _ptr(y), _ptr(z), n, total_steps, _ptr(charges), p,
             resolution, int(bool(use_curvature)), ctypes_byref(o),

@@ -89,7 +89,13 @@ typedef struct em_options {
     int warps_per_cta;    /* 0: automatic; else 1..32                        */
     int tile_charges;     /* 0: automatic; streamed-charge tile size         */
     int force_streamed;   /* 1: stream charge tiles even if they fit          */
+    int pack;             /* EM_PACK_*: pair loop form for fast FP32         */
 } em_options;
+
+/* ---- pair loop form (fast FP32 only) -------------------------------------- */
+#define EM_PACK_AUTO 0    /* library's choice                                */
+#define EM_PACK_SCALAR 1  /* one charge per FP32 instruction                 */
+#define EM_PACK_PAIRS 2   /* two charges per packed .f32x2 instruction       */
 
 /* Reference-compatible entry points (host pointers, synchronous).
  * Replace CalcField_CPU<float>/<double> (CPU_Implement.cpp:501-527): same
