@@ -48,7 +48,8 @@ class EmOptions(ctypes.Structure):
     _fields_ = [("arith", I), ("rule", I), ("require_n64", I),
                 ("device_ptrs", I), ("stream", P), ("threads_per_line", I),
                 ("warps_per_cta", I), ("tile_charges", I),
-                ("force_streamed", I), ("pack", I)]
+                ("force_streamed", I), ("pack", I),
+                ("lines_per_thread", I)]
 
 
 _SIGNATURES = {

@@ -59,6 +59,7 @@ template <class T> struct RefTraceParams {
 
 struct LaunchCfg {
     int tpl;     // threads per line (1, 2, 4, 8)
+    int kl;      // lines per lane (1, 2; 2 only for the fast scalar form)
     int warps;   // compute warps per CTA
     int grid;    // CTAs
     int resident;

@@ -52,26 +52,26 @@ inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
 // Relative cost of one line-group step for `tpl` threads per line: pair
 // work per lane plus the butterfly and the per-vertex step.
-inline double group_step_cost(long long p, int tpl)
+inline double group_step_cost(long long p, int tpl, int kl)
 {
     int lg = 0;
     for (int t = tpl; t > 1; t >>= 1)
         ++lg;
-    return (double)ceil_div(p, tpl) * 13.0 + 18.0 * lg + 120.0;
+    return kl * ((double)ceil_div(p, tpl) * 13.0 + 18.0 * lg + 120.0);
 }
 
 // Picks threads per line, compute warps per CTA and the grid for n lines
 // and p charges on a device with nsm SMs (one persistent CTA per SM).  The
 // model charges each SM sub-partition (4 per SM) for the warps it runs.
 inline void choose_shape(long long n, long long p, int nsm, int max_warps, int fixed_tpl,
-                         int *tpl_out, int *warps_out)
+                         int kl, int *tpl_out, int *warps_out)
 {
     double best = 0;
     int bt = 1, bw = 1;
     for (int tpl = 1; tpl <= 8; tpl <<= 1) {
         if (fixed_tpl && tpl != fixed_tpl)
             continue;
-        const long long lpw = 32 / tpl;
+        const long long lpw = kl * 32 / tpl;
         const long long groups = ceil_div(n, lpw);
         const long long grid = std::min<long long>(nsm, groups);
         const long long gpc = ceil_div(groups, grid);
@@ -83,7 +83,7 @@ inline void choose_shape(long long n, long long p, int nsm, int max_warps, int f
         // one warp per sub-partition cannot hide the FP32 pipe latency
         if (ceil_div(warps, 4) < 2)
             per_smsp *= 1.6;
-        const double t = per_smsp * group_step_cost(p, tpl);
+        const double t = per_smsp * group_step_cost(p, tpl, kl);
         if (best == 0 || t < best * 0.98) {
             best = t;
             bt = tpl;
@@ -106,15 +106,20 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     if (o.pack < EM_PACK_AUTO || o.pack > EM_PACK_PAIRS)
         return EM_ERR_ARG;
     int arith = o.arith == EM_ARITH_EXACT ? ARITH_EXACT : ARITH_FAST;
-    if (arith == ARITH_FAST && sizeof(T) == 4 && o.pack != EM_PACK_SCALAR)
+    // packed pairs only on request: each .f32x2 FMA holds the FMA pipe for
+    // two cycles, so it saves issue slots but not pipe time
+    if (arith == ARITH_FAST && sizeof(T) == 4 && o.pack == EM_PACK_PAIRS)
         arith = ARITH_FAST2;
+    if (o.lines_per_thread < 0 || o.lines_per_thread > 2)
+        return EM_ERR_ARG;
+    const int kl = (arith == ARITH_FAST && o.lines_per_thread == 2) ? 2 : 1;
     const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
     int tpl = 1, warps = 1;
     // resident if the padded set fits next to the barrier block
     const size_t gran_max = 16 * kUnroll;
     const size_t p_res = (p + gran_max - 1) / gran_max * gran_max;
     const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
-    choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, &tpl,
+    choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, kl, &tpl,
                  &warps);
     if (o.warps_per_cta)
         warps = std::min(o.warps_per_cta, resident ? 32 : 31);
@@ -122,8 +127,9 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     const int gran = tpl * kUnroll * (arith == ARITH_FAST2 ? 2 : 1);
     Plan r;
     r.arith = arith;
-    r.n_groups = ceil_div((long long)n, 32 / tpl);
+    r.n_groups = ceil_div((long long)n, kl * 32 / tpl);
     r.cfg.tpl = tpl;
+    r.cfg.kl = kl;
     r.cfg.warps = warps;
     r.cfg.grid = (int)std::min<long long>(c.nsm, r.n_groups);
     r.cfg.resident = resident ? 1 : 0;

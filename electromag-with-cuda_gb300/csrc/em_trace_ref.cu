@@ -239,11 +239,32 @@ __device__ __forceinline__ T line_reduce(T v)
     return v;
 }
 
-template <class T, int TPL, int ARITH>
-__global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams<T> P)
+// KL lines per lane (fast scalar form only): one broadcast charge load feeds
+// KL independent pair chains, which doubles the work in flight per warp.
+template <class T, int TPL, int ARITH, int KL, class Rec>
+__device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, const T *px,
+                                             const T *py, const T *pz, T K, bool three_arg,
+                                             Acc<T> *a)
+{
+    if (KL == 1) {
+        accumulate<T, TPL, ARITH>(tile, count, t, px[0], py[0], pz[0], K, three_arg, a[0]);
+    } else {
+#pragma unroll 4
+        for (int j = t; j < count; j += TPL) {
+            const auto c = load_charge(tile, j);
+#pragma unroll
+            for (int k = 0; k < KL; ++k)
+                pair_fast<T>(px[k], py[k], pz[k], c, a[k].x, a[k].y, a[k].z);
+        }
+    }
+}
+
+template <class T, int TPL, int ARITH, int KL, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams<T> P)
 {
     using Rec = typename ChargeRec<T>::type;
-    constexpr int LPW = 32 / TPL;
+    constexpr int LG = 32 / TPL;   // line slots per warp (lanes / TPL)
+    constexpr int LPW = LG * KL;   // lines per warp
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     Rec *tiles = reinterpret_cast<Rec *>(smem + 128);
@@ -324,34 +345,44 @@ __global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams
     // ---- compute warps --------------------------------------------------------
     uint32_t it = 0;
     for (int r = 0; r < rounds; ++r) {
-        const long long k = (long long)r * ncw + warp;
-        const long long g = blockIdx.x + (long long)gridDim.x * k;
-        const bool active = k < cta_groups;
-        const long long line = g * LPW + lane / TPL;
-        const bool own = active && line < P.n;
-        T px = 0, py = 0, pz = 0;
-        if (own) {
-            px = P.x[line];
-            py = P.y[line];
-            pz = P.z[line];
-        }
-        // SSE rule: the curvature vector is the seed, loaded once
-        // (CPU_Implement.cpp:254-256) and never updated.
-        T r0x = px, r0y = py, r0z = pz;
+        const long long gk = (long long)r * ncw + warp;
+        const long long g = blockIdx.x + (long long)gridDim.x * gk;
+        const bool active = gk < cta_groups;
         if (!streamed && !active)
             break;
+        long long line[KL];
+        bool own[KL];
+        T px[KL], py[KL], pz[KL], r0x[KL], r0y[KL], r0z[KL];
+#pragma unroll
+        for (int k = 0; k < KL; ++k) {
+            // slot k of the warp's lines: consecutive lanes -> consecutive lines
+            line[k] = g * LPW + k * LG + lane / TPL;
+            own[k] = active && line[k] < P.n;
+            px[k] = py[k] = pz[k] = 0;
+            if (own[k]) {
+                px[k] = P.x[line[k]];
+                py[k] = P.y[line[k]];
+                pz[k] = P.z[line[k]];
+            }
+            // SSE rule: the curvature vector is the seed, loaded once
+            // (CPU_Implement.cpp:254-256) and never updated.
+            r0x[k] = px[k];
+            r0y[k] = py[k];
+            r0z[k] = pz[k];
+        }
         for (int step = 1; step < P.total_steps; ++step) {
-            Acc<T> acc;
+            Acc<T> acc[KL];
             if (!streamed) {
-                accumulate<T, TPL, ARITH>(tiles, P.p_pad, t, px, py, pz, K, three_arg, acc);
+                accumulate_k<T, TPL, ARITH, KL>(tiles, P.p_pad, t, px, py, pz, K, three_arg,
+                                                acc);
             } else {
                 for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
                     const uint32_t s = it % NST, ph = (it / NST) & 1;
                     if (!mbar_wait(full0 + 8 * s, ph, P.err))
                         return;
                     if (active)
-                        accumulate<T, TPL, ARITH>(tiles + s * P.tile_recs, P.tile_recs, t, px,
-                                                  py, pz, K, three_arg, acc);
+                        accumulate_k<T, TPL, ARITH, KL>(tiles + s * P.tile_recs, P.tile_recs, t,
+                                                        px, py, pz, K, three_arg, acc);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(empty0 + 8 * s);
@@ -359,30 +390,34 @@ __global__ void __launch_bounds__(1024, 1) ref_trace_kernel(const RefTraceParams
                 if (!active)
                     continue;
             }
-            acc_finish<T, ARITH>(acc);
-            T ax = acc.x, ay = acc.y, az = acc.z;
-            if (TPL > 1) {
-                ax = line_reduce<T, TPL>(ax);
-                ay = line_reduce<T, TPL>(ay);
-                az = line_reduce<T, TPL>(az);
-            }
-            if (ARITH != ARITH_EXACT) {
-                ax = mul_rn(ax, K);
-                ay = mul_rn(ay, K);
-                az = mul_rn(az, K);
-            }
-            if (P.rule == RULE_GENERIC) {
-                // prevVec = previous point (CPU_Implement.cpp:148-153)
-                r0x = px;
-                r0y = py;
-                r0z = pz;
-            }
-            advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px, py, pz);
-            if (own && t == 0) {
-                const size_t idx = (size_t)step * n + (size_t)line;
-                store_stream(P.x + idx, px);
-                store_stream(P.y + idx, py);
-                store_stream(P.z + idx, pz);
+#pragma unroll
+            for (int k = 0; k < KL; ++k) {
+                acc_finish<T, ARITH>(acc[k]);
+                T ax = acc[k].x, ay = acc[k].y, az = acc[k].z;
+                if (TPL > 1) {
+                    ax = line_reduce<T, TPL>(ax);
+                    ay = line_reduce<T, TPL>(ay);
+                    az = line_reduce<T, TPL>(az);
+                }
+                if (ARITH != ARITH_EXACT) {
+                    ax = mul_rn(ax, K);
+                    ay = mul_rn(ay, K);
+                    az = mul_rn(az, K);
+                }
+                if (P.rule == RULE_GENERIC) {
+                    // prevVec = previous point (CPU_Implement.cpp:148-153)
+                    r0x[k] = px[k];
+                    r0y[k] = py[k];
+                    r0z[k] = pz[k];
+                }
+                advance<T>(ax, ay, az, r0x[k], r0y[k], r0z[k], curvature, P.resolution, px[k],
+                           py[k], pz[k]);
+                if (own[k] && t == 0) {
+                    const size_t idx = (size_t)step * n + (size_t)line[k];
+                    store_stream(P.x + idx, px[k]);
+                    store_stream(P.y + idx, py[k]);
+                    store_stream(P.z + idx, pz[k]);
+                }
             }
         }
     }
@@ -417,18 +452,33 @@ __global__ void stage_kernel(const T *raw, int p, T *staged, int p_pad, int pair
     }
 }
 
-template <class T, int TPL, int ARITH>
+template <class T, int TPL, int ARITH, int KL, int MAXT>
 cudaError_t launch_one(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
 {
-    auto kern = ref_trace_kernel<T, TPL, ARITH>;
+    auto kern = ref_trace_kernel<T, TPL, ARITH, KL, MAXT>;
+    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
+    if (threads > MAXT)
+        return cudaErrorInvalidConfiguration;
     cudaError_t e =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (e != cudaSuccess)
         return e;
-    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
     kern<<<cfg.grid, threads, cfg.smem, stream>>>(p);
     count_launch(1);
     return cudaGetLastError();
+}
+
+// Fast scalar form: KL lines per lane, register budget by thread bound
+// (1024 threads -> 64 registers, 768 -> 80).
+template <class T, int TPL>
+cudaError_t launch_fast(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
+{
+    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
+    if (cfg.kl == 2)
+        return threads <= 768 ? launch_one<T, TPL, ARITH_FAST, 2, 768>(p, cfg, stream)
+                              : launch_one<T, TPL, ARITH_FAST, 2, 1024>(p, cfg, stream);
+    return threads <= 768 ? launch_one<T, TPL, ARITH_FAST, 1, 768>(p, cfg, stream)
+                          : launch_one<T, TPL, ARITH_FAST, 1, 1024>(p, cfg, stream);
 }
 
 } // namespace
@@ -437,27 +487,29 @@ template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream)
 {
+    if (cfg.kl != 1 && (cfg.kl != 2 || arith != ARITH_FAST))
+        return cudaErrorInvalidValue;
     if (arith == ARITH_EXACT) {
         if (cfg.tpl != 1)
             return cudaErrorInvalidValue;
-        return launch_one<T, 1, ARITH_EXACT>(p, cfg, stream);
+        return launch_one<T, 1, ARITH_EXACT, 1, 1024>(p, cfg, stream);
     }
     if (arith == ARITH_FAST2) {
         if (sizeof(T) != 4)
             return cudaErrorInvalidValue;
         switch (cfg.tpl) {
-        case 1: return launch_one<T, 1, ARITH_FAST2>(p, cfg, stream);
-        case 2: return launch_one<T, 2, ARITH_FAST2>(p, cfg, stream);
-        case 4: return launch_one<T, 4, ARITH_FAST2>(p, cfg, stream);
-        case 8: return launch_one<T, 8, ARITH_FAST2>(p, cfg, stream);
+        case 1: return launch_one<T, 1, ARITH_FAST2, 1, 1024>(p, cfg, stream);
+        case 2: return launch_one<T, 2, ARITH_FAST2, 1, 1024>(p, cfg, stream);
+        case 4: return launch_one<T, 4, ARITH_FAST2, 1, 1024>(p, cfg, stream);
+        case 8: return launch_one<T, 8, ARITH_FAST2, 1, 1024>(p, cfg, stream);
         default: return cudaErrorInvalidValue;
         }
     }
     switch (cfg.tpl) {
-    case 1: return launch_one<T, 1, ARITH_FAST>(p, cfg, stream);
-    case 2: return launch_one<T, 2, ARITH_FAST>(p, cfg, stream);
-    case 4: return launch_one<T, 4, ARITH_FAST>(p, cfg, stream);
-    case 8: return launch_one<T, 8, ARITH_FAST>(p, cfg, stream);
+    case 1: return launch_fast<T, 1>(p, cfg, stream);
+    case 2: return launch_fast<T, 2>(p, cfg, stream);
+    case 4: return launch_fast<T, 4>(p, cfg, stream);
+    case 8: return launch_fast<T, 8>(p, cfg, stream);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -45,7 +45,8 @@ def _check(a, dtype_name):
 def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                arith="fast", rule="sse", require_n64=None, stream=None,
                threads_per_line=0, warps_per_cta=0, tile_charges=0,
-               force_streamed=False, pack="auto", plain=None):
+               force_streamed=False, pack="auto", lines_per_thread=0,
+               plain=None):
     """Traces n field lines in place; returns (rc, perf).
 
     rc is the reference's code (0 ok, 1 n == 0, 2 resolution == 0,
@@ -67,7 +68,8 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
         plain = (not device and arith == "fast" and rule == "sse"
                  and require_n64 in (None, True) and not threads_per_line
                  and not warps_per_cta and not tile_charges
-                 and not force_streamed and pack == "auto")
+                 and not force_streamed and pack == "auto"
+                 and not lines_per_thread)
     if plain:
         if device:
             raise ValueError("the plain entry point takes host arrays")
@@ -90,6 +92,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     o.tile_charges = tile_charges
     o.force_streamed = int(bool(force_streamed))
     o.pack = _PACK[pack]
+    o.lines_per_thread = lines_per_thread
     fn = lib.em_calc_field_ex_f32 if f32 else lib.em_calc_field_ex_f64
     rc = fn(_ptr(x), _ptr(y), _ptr(z), n, total_steps, _ptr(charges), p,
             resolution, int(bool(use_curvature)), ctypes_byref(o),

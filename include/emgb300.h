@@ -90,6 +90,7 @@ typedef struct em_options {
     int tile_charges;     /* 0: automatic; streamed-charge tile size         */
     int force_streamed;   /* 1: stream charge tiles even if they fit          */
     int pack;             /* EM_PACK_*: pair loop form for fast FP32         */
+    int lines_per_thread; /* 0: automatic; 1 or 2 (fast scalar form only)    */
 } em_options;
 
 /* ---- pair loop form (fast FP32 only) -------------------------------------- */

@@ -141,15 +141,17 @@ def first_approach(v, ch, radius):
     return out
 
 
-@pytest.mark.parametrize("pack", ["scalar", "pairs"])
+@pytest.mark.parametrize("pack,kl", [("scalar", 1), ("scalar", 2),
+                                     ("pairs", 1)])
 def test_fast_vertices_within_1e4_first_500_steps(em, gpu, orc, cpu_config,
-                                                  pack):
+                                                  pack, kl):
     ch, seeds, steps = cpu_config
     n = len(seeds)
     ref = lines_from(seeds, steps, np.float32)
     assert orc.calc_field(*ref, ch, n, 1.0, orc.CURV_SSE) == 0
     got = lines_from(seeds, steps, np.float32)
-    rc, perf = em.calc_field(*got, ch, n, 1.0, True, pack=pack)
+    rc, perf = em.calc_field(*got, ch, n, 1.0, True, pack=pack,
+                             lines_per_thread=kl)
     assert rc == 0
     R = np.stack([a.reshape(steps, n) for a in ref]).astype(np.float64)
     G = np.stack([a.reshape(steps, n) for a in got]).astype(np.float64)
@@ -165,28 +167,32 @@ def test_fast_vertices_within_1e4_first_500_steps(em, gpu, orc, cpu_config,
     assert perf.pairs == n * (steps - 1) * len(ch)
 
 
-@pytest.mark.parametrize("pack", ["scalar", "pairs"])
+@pytest.mark.parametrize("pack,kl", [("scalar", 1), ("scalar", 2),
+                                     ("pairs", 1)])
 @pytest.mark.parametrize("tpl", [1, 2, 4, 8])
-def test_fast_threads_per_line_variants_agree(em, gpu, golden, tpl, pack):
+def test_fast_threads_per_line_variants_agree(em, gpu, golden, tpl, pack, kl):
     name = "curv_f32"
     base = trace(em, golden, name, threads_per_line=1, pack="scalar")[2]
-    rc, _, v = trace(em, golden, name, threads_per_line=tpl, pack=pack)
+    rc, _, v = trace(em, golden, name, threads_per_line=tpl, pack=pack,
+                     lines_per_thread=kl)
     assert rc == 0
     err = np.abs(v.astype(np.float64) - base) / np.maximum(np.abs(base), 1)
     assert err[:, :8].max() <= VERTEX_RTOL
 
 
-@pytest.mark.parametrize("pack", ["scalar", "pairs"])
+@pytest.mark.parametrize("pack,kl", [("scalar", 1), ("scalar", 2),
+                                     ("pairs", 1)])
 @pytest.mark.parametrize("tpl", [1, 4])
-def test_fast_streamed_equals_resident_bitwise(em, gpu, cpu_config, tpl, pack):
+def test_fast_streamed_equals_resident_bitwise(em, gpu, cpu_config, tpl, pack,
+                                               kl):
     ch, seeds, _ = cpu_config
     n, steps = len(seeds), 60
     a = lines_from(seeds, steps, np.float32)
     b = lines_from(seeds, steps, np.float32)
     assert em.calc_field(*a, ch, n, 1.0, True, threads_per_line=tpl,
-                         pack=pack)[0] == 0
+                         pack=pack, lines_per_thread=kl)[0] == 0
     assert em.calc_field(*b, ch, n, 1.0, True, threads_per_line=tpl,
-                         pack=pack, force_streamed=True,
+                         pack=pack, lines_per_thread=kl, force_streamed=True,
                          tile_charges=64)[0] == 0
     for u, w in zip(a, b):
         assert np.array_equal(u, w)
