@@ -29,6 +29,7 @@ EM_ERR_TIMEOUT = 12
 EM_ERR_NO_DEVICE = 13
 EM_ERR_TOO_LARGE = 14
 
+EM_NOALLOC_MAX_CHARGES = 16384
 EM_ARITH_FAST = 0
 EM_ARITH_EXACT = 1
 EM_PACK_AUTO = 0
@@ -57,6 +58,7 @@ _SIGNATURES = {
     "em_calc_field_f64": (I, [P, P, P, S, S, P, S, D, I, P]),
     "em_calc_field_ex_f32": (I, [P, P, P, S, S, P, S, F, I, P, P]),
     "em_calc_field_ex_f64": (I, [P, P, P, S, S, P, S, D, I, P, P]),
+    "em_calc_field_noalloc_f32": (I, [P, P, P, S, S, P, S, F, I, P]),
     "em_field_f32": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_field_f64": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_fp32_peak_tflops": (I, [P, P]),

@@ -121,6 +121,26 @@ EM_API int em_calc_field_ex_f64(double *x, double *y, double *z, size_t n,
                          double resolution, int use_curvature,
                          const em_options *opt, em_perf *perf);
 
+/* Tracing without any device allocation by the library.  This entry point
+ * has no counterpart in the reference (whose calc-field paths allocate and
+ * own their buffers).  It is for callers that cannot let a library call
+ * cudaMalloc: applications whose own pool holds the whole GPU, and loops
+ * that cannot take the device-wide synchronisation an allocation may cause.
+ * x, y, z (n*total_steps each, reference layout) and charges
+ * (p records {x,y,z,q}, 16-B aligned) are DEVICE pointers; the work runs on
+ * `stream` (NULL: the default stream) and the call returns when it is done.
+ * Default options: fast FP32, the SSE stepping rule, any n.
+ * Its scratch is one static device array per GPU, held until exit, sized
+ * for at most EM_NOALLOC_MAX_CHARGES charges; larger sets return
+ * EM_ERR_TOO_LARGE.  The first call on a device performs a one-time set-up
+ * (make it before any stream capture).  All calls on a device share the
+ * array: calls that overlap on the GPU race, so order them. */
+#define EM_NOALLOC_MAX_CHARGES 16384
+EM_API int em_calc_field_noalloc_f32(float *x, float *y, float *z, size_t n,
+                                     size_t total_steps, const float *charges,
+                                     size_t p, float resolution,
+                                     int use_curvature, void *stream);
+
 /* Field at m points, no stepping: E_i = sum_j PartField(charge_j, point_i)
  * summed in charge order (include/Electrostatics.h:38-60 as
  * CPU_Implement.cpp:274-320 sums it).  Points are SoA px/py/pz; the result
