@@ -44,6 +44,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    # launch-shape overrides (0/auto = the library's choice); for profiling
+    ap.add_argument("--tpl", type=int, default=0)
+    ap.add_argument("--kl", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--pack", default="auto")
     return ap.parse_args()
 
 
@@ -214,9 +219,12 @@ def main():
         X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c])).to(dev)
     dch = torch.from_numpy(ch).to(dev)
 
+    shape = dict(threads_per_line=args.tpl, lines_per_thread=args.kl,
+                 warps_per_cta=args.warps, pack=args.pack)
+
     def step():
         rc, perf = em.calc_field(*X, dch, n, 1.0, True, require_n64=False,
-                                 stream=stream.cuda_stream)
+                                 stream=stream.cuda_stream, **shape)
         if rc:
             raise em.EmError(rc, "em_calc_field_ex_f32")
         return perf

@@ -35,6 +35,11 @@ EM_ARITH_EXACT = 1
 EM_PACK_AUTO = 0
 EM_PACK_SCALAR = 1
 EM_PACK_PAIRS = 2
+EM_PREC_FP32 = 0
+EM_PREC_MIXED = 1
+EM_TERM_STEPS = 0
+EM_TERM_CHARGE = 1
+EM_TERM_NULL = 2
 EM_RULE_SSE = 0
 EM_RULE_GENERIC = 1
 
@@ -42,7 +47,7 @@ EM_RULE_GENERIC = 1
 class EmPerf(ctypes.Structure):
     """em_perf: perfPacket's fields ("Data Structures.h":221-236) + counters."""
     _fields_ = [("performance", D), ("time", D), ("progress", D),
-                ("pairs", D), ("wall_time", D)]
+                ("pairs", D), ("wall_time", D), ("fp64_refines", D)]
 
 
 class EmOptions(ctypes.Structure):
@@ -50,7 +55,8 @@ class EmOptions(ctypes.Structure):
                 ("device_ptrs", I), ("stream", P), ("threads_per_line", I),
                 ("warps_per_cta", I), ("tile_charges", I),
                 ("force_streamed", I), ("pack", I),
-                ("lines_per_thread", I)]
+                ("lines_per_thread", I), ("precision", I),
+                ("null_frac", D)]
 
 
 _SIGNATURES = {
@@ -59,6 +65,11 @@ _SIGNATURES = {
     "em_calc_field_ex_f32": (I, [P, P, P, S, S, P, S, F, I, P, P]),
     "em_calc_field_ex_f64": (I, [P, P, P, S, S, P, S, D, I, P, P]),
     "em_calc_field_noalloc_f32": (I, [P, P, P, S, S, P, S, F, I, P]),
+    "em_trace_lines_f32": (I, [P, P, P, S, S, P, P, S, F, F, P, P, P, P, P,
+                               P, P]),
+    "em_trace_lines_f64": (I, [P, P, P, S, S, P, P, S, D, D, P, P, P, P, P,
+                               P, P]),
+    "em_seed_fibonacci_f32": (I, [P, S, S, F, P, P, P, S, P]),
     "em_field_f32": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_field_f64": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_fp32_peak_tflops": (I, [P, P]),

@@ -161,7 +161,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         e = cudaMemcpyAsync(c.charges_raw, charges, p * rec, kin, s);
     if (e == cudaSuccess)
         e = launch_stage_charges<T>(c.charges_raw, (int)p, c.charges, pl.p_pad,
-                                    pl.arith == ARITH_FAST2, s);
+                                    stage_layout(pl.arith), pl.cfg.tile_recs, s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(c.err, 0, sizeof(int), s);
     if (e == cudaSuccess && !o.device_ptrs) {

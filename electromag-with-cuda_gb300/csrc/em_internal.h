@@ -57,9 +57,44 @@ template <class T> struct RefTraceParams {
     int *err;                  // device error word
 };
 
+// Extended tracer (em_trace_ext.cu).
+enum ExtMode : int {
+    EXT_FAST = 0,  // T arithmetic throughout (float, or double = the FP64 path)
+    EXT_MIXED = 1, // FP32 pairs + corrected inv^3 + compensation, FP64 position
+};
+// termination classes written by the kernel (same values as EM_TERM_*)
+constexpr int EM_TERM_STEPS_DEV = 0;
+constexpr int EM_TERM_CHARGE_DEV = 1;
+constexpr int EM_TERM_NULL_DEV = 2;
+
+template <class T> struct ExtParams {
+    T *x, *y, *z;                   // n*max_steps each; row 0 = seeds
+    T *ex, *ey, *ez;                // optional: field at each evaluated vertex
+    const void *charges;            // staged negatives-first, p_pad records
+    const int *meta;                // [0] = padded negative block size
+    const float *qabs;              // largest |q|
+    long long n;
+    int max_steps;
+    const int *steps_per_line;      // optional per-line limits
+    double resolution;
+    double term_r2;
+    double null_frac;
+    int *len, *cls;
+    unsigned long long *next_line, *evals, *refines;
+    int p_pad, n_tiles, tile_recs, stages, resident;
+    int *err;
+};
+
+template <class T>
+cudaError_t launch_ext_stage(const void *raw, int p, void *staged, int p_pad, int gran,
+                             int *meta, float *qabs, cudaStream_t stream);
+template <class T>
+cudaError_t launch_ext_trace(const ExtParams<T> &p, const struct LaunchCfg &cfg, int mode,
+                             cudaStream_t stream);
+
 struct LaunchCfg {
     int tpl;     // threads per line (1, 2, 4, 8)
-    int kl;      // lines per lane (1, 2; 2 only for the fast scalar form)
+    int kl;      // lines per lane (1, 2; 2 only for the fast forms)
     int warps;   // compute warps per CTA
     int grid;    // CTAs
     int resident;
@@ -76,10 +111,11 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, i
                              cudaStream_t stream);
 
 // Stages p raw charge records into p_pad records (pad record {1e15, 1e15,
-// 1e15, 0}, whose contribution is exactly zero), plain or pair-interleaved.
+// 1e15, 0}, whose contribution is exactly zero), plain (paired = 0) or in
+// the packed form's two-plane blocks of `block` records (1).
 template <class T>
 cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad, int paired,
-                                 cudaStream_t stream);
+                                 int block, cudaStream_t stream);
 
 // Adds k to the process-wide count of kernels launched by this library.
 void count_launch(unsigned long long k);

@@ -126,7 +126,7 @@ extern "C" int em_calc_field_noalloc_f32(float *x, float *y, float *z, size_t n,
     cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
     if (e == cudaSuccess)
         e = launch_stage_charges<float>(charges, (int)p, staged, pl.p_pad,
-                                        pl.arith == ARITH_FAST2, s);
+                                        stage_layout(pl.arith), pl.cfg.tile_recs, s);
     RefTraceParams<float> prm{};
     prm.x = x;
     prm.y = y;

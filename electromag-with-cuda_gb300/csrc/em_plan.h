@@ -50,6 +50,9 @@ struct Plan {
 
 inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
+// Staged charge layout for a kernel arithmetic (stage_kernel's `paired`).
+inline int stage_layout(int arith) { return arith == ARITH_FAST2 ? 1 : 0; }
+
 // Relative cost of one line-group step for `tpl` threads per line: pair
 // work per lane plus the butterfly and the per-vertex step.
 inline double group_step_cost(long long p, int tpl, int kl)
@@ -112,7 +115,11 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
         arith = ARITH_FAST2;
     if (o.lines_per_thread < 0 || o.lines_per_thread > 2)
         return EM_ERR_ARG;
-    const int kl = (arith == ARITH_FAST && o.lines_per_thread == 2) ? 2 : 1;
+    // lines per lane: 2 for the fast forms when the caller does not say (one
+    // charge load feeds two independent chains), 1 for exact arithmetic
+    int kl = 1;
+    if (arith != ARITH_EXACT)
+        kl = o.lines_per_thread ? o.lines_per_thread : 2;
     const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
     int tpl = 1, warps = 1;
     // resident if the padded set fits next to the barrier block

@@ -1,0 +1,674 @@
+// Extended field-line tracer: lines seeded around charges, stopped within a
+// radius of a negative charge, at a zero/invalid field or at a per-line step
+// limit.  The stepping rule is the reference's (CPU_Implement.cpp:322-338:
+// curvature against the line's seed, unit field step scaled by 1/(k+1)).
+//
+// Work decomposition.  A lane group (TPL lanes) owns one line at a time and
+// splits its charge sum; the warp's groups advance in lockstep, one field
+// evaluation per step-iteration.  When lines end, the warp ballots its
+// finished groups and takes that many new lines from a device work queue
+// with a single atomic (warp-ballot compaction), so lanes never idle while
+// lines remain.
+//
+// Charges are staged negatives-first, each block padded to the loop granule:
+// only the negative block tracks the nearest negative charge (one FMNMX per
+// pair).  Charges sit in shared memory: staged once when they fit, otherwise
+// streamed through a ring of tiles by a producer warp, with the CTA stepping
+// in lockstep (one CTA-wide vote per step-iteration decides whether any line
+// is left).
+//
+// Precision modes (template MODE):
+//   EXT_FAST   T = float or double: r^2 by FMA, reciprocal square root,
+//              s = q inv^3, a += s r.  With T = double this is the all-FP64
+//              path.
+//   EXT_MIXED  T = float pair sums with a first-order Newton correction of
+//              inv^3 (s = s0 (2.5 - 1.5 r^2 inv^2), removing the rsqrt error
+//              to first order), two-sum compensated accumulation across
+//              chunks of 64 charges and across lanes, the line position in
+//              FP64, and an FP64 re-evaluation of the whole field where
+//              |E| < null_frac * (largest single contribution bound).
+#include "em_device.cuh"
+#include "em_internal.h"
+#include "em_math.cuh"
+
+namespace em {
+namespace {
+
+constexpr int kChunk = 64; // pairs per lane between compensated additions
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float ap = __fsub_rn(s, bp);
+    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+// Compensated value (hi, lo).
+struct CF {
+    float h = 0, l = 0;
+    __device__ __forceinline__ void add(float v)
+    {
+        float e;
+        two_sum(h, v, h, e);
+        l = __fadd_rn(l, e);
+    }
+};
+
+template <class T> struct ExtLane {
+    T px, py, pz;         // evaluation point (FP32 copy in mixed mode)
+    double dx, dy, dz;    // mixed: FP64 position accumulator
+};
+
+// ---------------------------------------------------------------------------
+// Staging: stable partition of p raw records into
+//   [negatives | pad to gran][positives | pad to p_pad], one CTA of 1024.
+// meta[0] = size of the padded negative block (records).
+// qabs[0] = largest |q| (float), for the mixed mode's contribution bound.
+template <class T>
+__global__ void __launch_bounds__(1024)
+    ext_stage_kernel(const T *raw, int p, T *staged, int p_pad, int gran, int *meta, float *qabs)
+{
+    __shared__ int scan[1024];
+    __shared__ float qm[32];
+    const int tid = threadIdx.x;
+    const int per = (p + 1023) / 1024;
+    const int b = tid * per, e = min(p, b + per);
+    int neg = 0;
+    float qmax = 0;
+    for (int i = b; i < e; ++i) {
+        const T q = raw[4 * (size_t)i + 3];
+        neg += q < T(0);
+        qmax = fmaxf(qmax, fabsf((float)q));
+    }
+    scan[tid] = neg;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int v = tid >= off ? scan[tid - off] : 0;
+        __syncthreads();
+        scan[tid] += v;
+        __syncthreads();
+    }
+    const int total_neg = scan[1023];
+    const int neg_pad = (total_neg + gran - 1) / gran * gran;
+    int wn = scan[tid] - neg;       // negatives before this chunk
+    int wp = neg_pad + (b - wn);    // positives go after the padded block
+    if (b > p)
+        wp = neg_pad;
+    for (int i = b; i < e; ++i) {
+        const T *r = raw + 4 * (size_t)i;
+        T *d = staged + 4 * (size_t)(r[3] < T(0) ? wn++ : wp++);
+        d[0] = r[0];
+        d[1] = r[1];
+        d[2] = r[2];
+        d[3] = r[3];
+    }
+    // pad records {1e15, 1e15, 1e15, 0}: exactly zero contribution
+    const int pos_end = neg_pad + (p - total_neg);
+    for (int i = tid; i < p_pad; i += 1024) {
+        if ((i >= total_neg && i < neg_pad) || i >= pos_end) {
+            T *d = staged + 4 * (size_t)i;
+            d[0] = d[1] = d[2] = T(1e15);
+            d[3] = T(0);
+        }
+    }
+    for (int o = 16; o; o >>= 1)
+        qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, o));
+    if ((tid & 31) == 0)
+        qm[tid >> 5] = qmax;
+    __syncthreads();
+    if (tid == 0) {
+        float m = 0;
+        for (int w = 0; w < 32; ++w)
+            m = fmaxf(m, qm[w]);
+        meta[0] = neg_pad;
+        *qabs = m;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pair loops over shared-memory records [0, count) of one tile, lane t of
+// TPL; [0, jneg) are negative charges (nearest one tracked).
+template <int TPL>
+__device__ __forceinline__ void pairs_fast(const float4 *tile, int jneg, int count, int t,
+                                           float px, float py, float pz, float &ax, float &ay,
+                                           float &az, float &dneg)
+{
+#pragma unroll 4
+    for (int j = t; j < jneg; j += TPL) {
+        const float4 c = tile[j];
+        const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        dneg = fminf(dneg, r2);
+        const float inv = rsqrt_fast(r2);
+        const float s = (c.w * inv) * (inv * inv);
+        ax = fmaf(s, dx, ax);
+        ay = fmaf(s, dy, ay);
+        az = fmaf(s, dz, az);
+    }
+#pragma unroll 8
+    for (int j = jneg + t; j < count; j += TPL) {
+        const float4 c = tile[j];
+        const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float inv = rsqrt_fast(r2);
+        const float s = (c.w * inv) * (inv * inv);
+        ax = fmaf(s, dx, ax);
+        ay = fmaf(s, dy, ay);
+        az = fmaf(s, dz, az);
+    }
+}
+
+template <int TPL>
+__device__ __forceinline__ void pairs_fast(const ChargeD *tile, int jneg, int count, int t,
+                                           double px, double py, double pz, double &ax,
+                                           double &ay, double &az, double &dneg)
+{
+    for (int j = t; j < count; j += TPL) {
+        const double2 *r = reinterpret_cast<const double2 *>(tile + j);
+        const double2 a = r[0], b = r[1];
+        const double dx = px - a.x, dy = py - a.y, dz = pz - b.x;
+        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+        if (j < jneg)
+            dneg = fmin(dneg, r2);
+        const double inv = rsqrt(r2);
+        const double s = (b.y * inv) * (inv * inv);
+        ax = fma(s, dx, ax);
+        ay = fma(s, dy, ay);
+        az = fma(s, dz, az);
+    }
+}
+
+// Mixed: FP32 pairs with the inv^3 correction over records [lo, hi) (lo a
+// multiple of TPL), compensated every kChunk pairs; dmin gets the nearest
+// distance^2 of the range.
+template <int TPL>
+__device__ __forceinline__ void mixed_range(const float4 *tile, int lo, int hi, int t, float px,
+                                            float py, float pz, CF &hx, CF &hy, CF &hz,
+                                            float &dmin)
+{
+    for (int j0 = lo + t; j0 < hi; j0 += TPL * kChunk) {
+        const int j1 = min(hi, j0 + TPL * kChunk);
+        float ax = 0, ay = 0, az = 0;
+#pragma unroll 4
+        for (int j = j0; j < j1; j += TPL) {
+            const float4 c = tile[j];
+            const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            dmin = fminf(dmin, r2);
+            const float inv = rsqrt_fast(r2);
+            const float inv2 = inv * inv;
+            const float s0 = (c.w * inv) * inv2;
+            // inv^3 carries three times the relative error eps of inv; to
+            // first order r2 inv2 - 1 = 2 eps, so s0 (2.5 - 1.5 r2 inv2) =
+            // s0 / (1 + 3 eps): one Newton correction, three FMA-pipe ops
+            const float g = fmaf(-1.5f * r2, inv2, 2.5f);
+            const float sc = s0 * g;
+            ax = fmaf(sc, dx, ax);
+            ay = fmaf(sc, dy, ay);
+            az = fmaf(sc, dz, az);
+        }
+        hx.add(ax);
+        hy.add(ay);
+        hz.add(az);
+    }
+}
+
+template <int TPL>
+__device__ __forceinline__ void pairs_mixed(const float4 *tile, int jneg, int count, int t,
+                                            float px, float py, float pz, CF &hx, CF &hy, CF &hz,
+                                            float &dneg, float &dall)
+{
+    float dn = 3.0e38f, dp = 3.0e38f;
+    mixed_range<TPL>(tile, 0, jneg, t, px, py, pz, hx, hy, hz, dn);
+    mixed_range<TPL>(tile, jneg, count, t, px, py, pz, hx, hy, hz, dp);
+    dneg = fminf(dneg, dn);
+    dall = fminf(dall, fminf(dn, dp));
+}
+
+// FP64 field at (px, py, pz) from the staged records in global memory, lane
+// t of TPL (summed later across the group).
+template <int TPL>
+__device__ __forceinline__ void field_fp64(const float4 *charges, int count, int t, double px,
+                                           double py, double pz, double &ax, double &ay,
+                                           double &az)
+{
+    for (int j = t; j < count; j += TPL) {
+        const float4 c = charges[j];
+        const double dx = px - (double)c.x, dy = py - (double)c.y, dz = pz - (double)c.z;
+        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+        const double inv = 1.0 / sqrt(r2);
+        const double s = (double)c.w * inv * inv * inv;
+        ax = fma(s, dx, ax);
+        ay = fma(s, dy, ay);
+        az = fma(s, dz, az);
+    }
+}
+
+template <class T, int TPL>
+__device__ __forceinline__ T group_min(T v)
+{
+#pragma unroll
+    for (int o = TPL / 2; o >= 1; o >>= 1)
+        v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <int TPL>
+__device__ __forceinline__ void group_two_sum(CF &c)
+{
+#pragma unroll
+    for (int o = TPL / 2; o >= 1; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, c.h, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, c.l, o);
+        // both partners compute the same sum: order the operands by lane
+        // half so the bits agree
+        float a = c.h, b = oh, la = c.l, lb = ol;
+        if ((threadIdx.x & o) != 0) {
+            a = oh;
+            b = c.h;
+            la = ol;
+            lb = c.l;
+        }
+        float s, e;
+        two_sum(a, b, s, e);
+        c.h = s;
+        c.l = __fadd_rn(__fadd_rn(la, lb), e);
+    }
+}
+
+template <class T, int TPL>
+__device__ __forceinline__ T group_sum(T v)
+{
+#pragma unroll
+    for (int o = TPL / 2; o >= 1; o >>= 1) {
+        const T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (threadIdx.x & o) ? w + v : v + w;
+    }
+    return v;
+}
+
+// Step vector of the reference rule (CPU_Implement.cpp:327-331): returns
+// E / ((k+1) res |E|) with the reference's IEEE sequence; k2 = |E|^2.
+template <class T>
+__device__ __forceinline__ void step_vector(T ex, T ey, T ez, T r0x, T r0y, T r0z, T res, T &sx,
+                                            T &sy, T &sz, T &k2)
+{
+    k2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
+    const T ix = sub_rn(ex, r0x), iy = sub_rn(ey, r0y), iz = sub_rn(ez, r0z);
+    const T cx = sub_rn(mul_rn(iy, r0z), mul_rn(iz, r0y));
+    const T cy = sub_rn(mul_rn(iz, r0x), mul_rn(ix, r0z));
+    const T cz = sub_rn(mul_rn(ix, r0y), mul_rn(iy, r0x));
+    const T c2 = add_rn(add_rn(mul_rn(cx, cx), mul_rn(cy, cy)), mul_rn(cz, cz));
+    const T kc = div_rn(sqrt_rn(c2), mul_rn(k2, sqrt_rn(k2)));
+    const T s = mul_rn(mul_rn(add_rn(kc, T(1)), res), sqrt_rn(k2));
+    sx = div_rn(ex, s);
+    sy = div_rn(ey, s);
+    sz = div_rn(ez, s);
+}
+
+template <class T, int TPL, int MODE>
+__global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P)
+{
+    using Rec = typename ChargeRec<T>::type;
+    constexpr int LG = 32 / TPL; // line slots per warp
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    Rec *tiles = reinterpret_cast<Rec *>(smem + 128);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const bool streamed = !P.resident;
+    const int ncw = streamed ? nwarps - 1 : nwarps;
+    const int NST = streamed ? P.stages : 1;
+    if (NST > 8 || ncw < 1) {
+        if (threadIdx.x == 0)
+            atomicCAS(P.err, 0, EM_DEVERR_CONFIG);
+        return;
+    }
+    const uint32_t full0 = smem_addr(bars), empty0 = smem_addr(bars + 8);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, ncw);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int jneg_all = *P.meta; // padded negative block (records)
+    const float qabs_max = *P.qabs; // largest |q|
+    const T K = (T)kElectroK;
+    const T term_r2 = (T)P.term_r2;
+    const size_t n = (size_t)P.n;
+
+    if (!streamed) {
+        if (threadIdx.x == 0) {
+            const uint32_t bytes = (uint32_t)P.p_pad * (uint32_t)sizeof(Rec);
+            mbar_arrive_expect_tx(full0, bytes);
+            const char *src = static_cast<const char *>(P.charges);
+            const uint32_t dst = smem_addr(tiles);
+            constexpr uint32_t CH = 32768;
+            for (uint32_t off = 0; off < bytes; off += CH)
+                bulk_g2s(dst + off, src + off, bytes - off < CH ? bytes - off : CH, full0);
+        }
+        if (!mbar_wait(full0, 0, P.err))
+            return;
+    }
+
+    if (streamed && warp == nwarps - 1) {
+        // ---- producer: tiles of every step-iteration while any line lives ---
+        const uint32_t tb = (uint32_t)P.tile_recs * (uint32_t)sizeof(Rec);
+        const char *src = static_cast<const char *>(P.charges);
+        uint32_t it = 0;
+        bool ok = true;
+        while (__syncthreads_or(0)) {
+            if (lane == 0 && ok && *(volatile int *)P.err == 0) {
+                for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+                    const uint32_t s = it % NST, ph = (it / NST) & 1;
+                    if (it >= (uint32_t)NST && !mbar_wait(empty0 + 8 * s, ph ^ 1, P.err)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(full0 + 8 * s, tb);
+                    bulk_g2s(smem_addr(tiles) + s * tb, src + (size_t)tile * tb, tb,
+                             full0 + 8 * s);
+                }
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            for (uint32_t k = 0; k < (uint32_t)NST && k < it; ++k) {
+                const uint32_t j = it - 1 - k;
+                mbar_wait(full0 + 8 * (j % NST), (j / NST) & 1, P.err);
+            }
+        }
+        return;
+    }
+
+    // ---- line slots ------------------------------------------------------------
+    const int t = lane % TPL;
+    const int grp_leader = lane - t;
+    const long long total_slots = (long long)gridDim.x * ncw * LG;
+    long long line = ((long long)blockIdx.x * ncw + warp) * LG + lane / TPL;
+    int s = 1, lim = 0;
+    ExtLane<T> st;
+    st.px = st.py = st.pz = 0;
+    st.dx = st.dy = st.dz = 0;
+    unsigned long long evals = 0, refines = 0;
+
+    // Loads line `l`'s seed and limit; returns false if the line needs no
+    // evaluation (limit < 2), after recording its result.
+    auto start_line = [&](long long l) -> bool {
+        st.px = P.x[l];
+        st.py = P.y[l];
+        st.pz = P.z[l];
+        st.dx = (double)st.px;
+        st.dy = (double)st.py;
+        st.dz = (double)st.pz;
+        lim = P.max_steps;
+        if (P.steps_per_line)
+            lim = max(1, min(P.steps_per_line[l], P.max_steps));
+        s = 1;
+        if (lim < 2) {
+            if (t == 0) {
+                P.len[l] = 1;
+                P.cls[l] = EM_TERM_STEPS_DEV;
+            }
+            return false;
+        }
+        return true;
+    };
+
+    bool live = line < P.n && start_line(line);
+    bool need = line < P.n && !live; // slot needs a new line
+    if (line >= P.n)
+        line = -1;
+    // refill (warp-ballot): finished slots take new lines with one atomic
+    auto refill = [&]() {
+        for (int guard = 0; guard < 1 << 20; ++guard) {
+            const unsigned m = __ballot_sync(0xffffffffu, t == 0 && need);
+            if (!m)
+                break;
+            const int first = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == first)
+                base = atomicAdd(P.next_line, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, first);
+            const long long mine =
+                (long long)(base + __popc(m & ((1u << lane) - 1u))) + total_slots;
+            const long long nl = __shfl_sync(0xffffffffu, mine, grp_leader);
+            if (need) {
+                if (nl < P.n) {
+                    line = nl;
+                    live = start_line(line);
+                    need = !live;
+                } else {
+                    line = -1;
+                    live = false;
+                    need = false;
+                }
+            }
+        }
+    };
+    refill();
+
+    uint32_t it = 0;
+    bool failed = false;
+    for (;;) {
+        const bool any = streamed ? __syncthreads_or(live) != 0 : __any_sync(0xffffffffu, live);
+        if (!any)
+            break;
+        // ---- field (and nearest negative charge) at the current vertex -----
+        T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
+        float dall = 3.0e38f;
+        CF hx, hy, hz;
+        if (!streamed) {
+            if constexpr (MODE == EXT_MIXED)
+                pairs_mixed<TPL>(tiles, jneg_all, P.p_pad, t, st.px, st.py, st.pz, hx, hy, hz,
+                                 dneg, dall);
+            else
+                pairs_fast<TPL>(tiles, jneg_all, P.p_pad, t, st.px, st.py, st.pz, ax, ay, az,
+                                dneg);
+        } else {
+            for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+                const uint32_t sg = it % NST, ph = (it / NST) & 1;
+                // on a failed wait the warp stops computing but keeps voting,
+                // so the CTA-wide loop still ends for every thread
+                if (!failed && !mbar_wait(full0 + 8 * sg, ph, P.err))
+                    failed = true;
+                if (!failed) {
+                    const int base = tile * P.tile_recs;
+                    const int jn = min(max(jneg_all - base, 0), P.tile_recs);
+                    const Rec *tp = tiles + sg * P.tile_recs;
+                    if constexpr (MODE == EXT_MIXED)
+                        pairs_mixed<TPL>(tp, jn, P.tile_recs, t, st.px, st.py, st.pz, hx, hy,
+                                         hz, dneg, dall);
+                    else
+                        pairs_fast<TPL>(tp, jn, P.tile_recs, t, st.px, st.py, st.pz, ax, ay,
+                                        az, dneg);
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(empty0 + 8 * sg);
+                }
+            }
+            if (failed) {
+                live = false;
+                need = false;
+                line = -1;
+                continue;
+            }
+        }
+        // ---- combine the group's lanes -------------------------------------
+        if constexpr (MODE == EXT_MIXED) {
+            group_two_sum<TPL>(hx);
+            group_two_sum<TPL>(hy);
+            group_two_sum<TPL>(hz);
+            ax = (T)__fadd_rn(hx.h, hx.l);
+            ay = (T)__fadd_rn(hy.h, hy.l);
+            az = (T)__fadd_rn(hz.h, hz.l);
+            dall = group_min<float, TPL>(dall);
+        } else {
+            ax = group_sum<T, TPL>(ax);
+            ay = group_sum<T, TPL>(ay);
+            az = group_sum<T, TPL>(az);
+        }
+        dneg = group_min<T, TPL>(dneg);
+        ax = mul_rn(ax, K);
+        ay = mul_rn(ay, K);
+        az = mul_rn(az, K);
+
+        if constexpr (MODE == EXT_MIXED) {
+            // near a null |E| is far below its largest term and the FP32 sum
+            // loses its digits: redo the field in FP64 there
+            const float bound = qabs_max * (float)kElectroK / dall;
+            const float e2 = ax * ax + ay * ay + az * az;
+            const float lim2 = (float)P.null_frac * bound;
+            const bool redo = live && !(e2 >= lim2 * lim2);
+            if (__any_sync(0xffffffffu, redo)) {
+                double fx = 0, fy = 0, fz = 0;
+                if (redo)
+                    field_fp64<TPL>(reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
+                                    (double)(float)st.px, (double)(float)st.py,
+                                    (double)(float)st.pz, fx, fy, fz);
+                fx = group_sum<double, TPL>(fx);
+                fy = group_sum<double, TPL>(fy);
+                fz = group_sum<double, TPL>(fz);
+                if (redo) {
+                    ax = (T)(fx * kElectroK);
+                    ay = (T)(fy * kElectroK);
+                    az = (T)(fz * kElectroK);
+                    refines += (t == 0);
+                }
+            }
+        }
+        if (live) {
+            evals += (t == 0);
+            const size_t row = (size_t)(s - 1) * n + (size_t)line;
+            if (P.ex && t == 0) {
+                P.ex[row] = ax;
+                P.ey[row] = ay;
+                P.ez[row] = az;
+            }
+            int cls = -1;
+            if (dneg < term_r2) {
+                cls = EM_TERM_CHARGE_DEV;
+            } else {
+                const T r0x = ld_seed(P.x + line), r0y = ld_seed(P.y + line),
+                        r0z = ld_seed(P.z + line);
+                T sx, sy, sz, k2;
+                step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
+                T nx, ny, nz;
+                if constexpr (MODE == EXT_MIXED) {
+                    st.dx += (double)sx;
+                    st.dy += (double)sy;
+                    st.dz += (double)sz;
+                    nx = (T)st.dx;
+                    ny = (T)st.dy;
+                    nz = (T)st.dz;
+                } else {
+                    nx = add_rn(st.px, sx);
+                    ny = add_rn(st.py, sy);
+                    nz = add_rn(st.pz, sz);
+                }
+                if (!(k2 > T(0)) || !isfinite(nx) || !isfinite(ny) || !isfinite(nz)) {
+                    cls = EM_TERM_NULL_DEV;
+                } else {
+                    st.px = nx;
+                    st.py = ny;
+                    st.pz = nz;
+                    const size_t w = (size_t)s * n + (size_t)line;
+                    if (t == 0) {
+                        store_stream(P.x + w, nx);
+                        store_stream(P.y + w, ny);
+                        store_stream(P.z + w, nz);
+                    }
+                    ++s;
+                    if (s >= lim)
+                        cls = EM_TERM_STEPS_DEV;
+                }
+            }
+            if (cls >= 0) {
+                if (t == 0) {
+                    P.len[line] = s;
+                    P.cls[line] = cls;
+                }
+                live = false;
+                need = true;
+            }
+        }
+        refill();
+    }
+    // counters: one atomic per warp
+    for (int o = 16; o; o >>= 1) {
+        evals += __shfl_xor_sync(0xffffffffu, evals, o);
+        refines += __shfl_xor_sync(0xffffffffu, refines, o);
+    }
+    if (lane == 0) {
+        atomicAdd(P.evals, evals);
+        if (refines)
+            atomicAdd(P.refines, refines);
+    }
+}
+
+template <class T, int TPL, int MODE>
+cudaError_t launch_ext_one(const ExtParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
+{
+    auto kern = ext_trace_kernel<T, TPL, MODE>;
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess)
+        return e;
+    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
+    kern<<<cfg.grid, threads, cfg.smem, stream>>>(p);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template <class T, int MODE>
+cudaError_t launch_ext_mode(const ExtParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
+{
+    switch (cfg.tpl) {
+    case 4: return launch_ext_one<T, 4, MODE>(p, cfg, stream);
+    case 8: return launch_ext_one<T, 8, MODE>(p, cfg, stream);
+    case 16: return launch_ext_one<T, 16, MODE>(p, cfg, stream);
+    case 32: return launch_ext_one<T, 32, MODE>(p, cfg, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace
+
+template <class T>
+cudaError_t launch_ext_stage(const void *raw, int p, void *staged, int p_pad, int gran,
+                             int *meta, float *qabs, cudaStream_t stream)
+{
+    ext_stage_kernel<T><<<1, 1024, 0, stream>>>(static_cast<const T *>(raw), p,
+                                                static_cast<T *>(staged), p_pad, gran, meta,
+                                                qabs);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_ext_trace<float>(const ExtParams<float> &p, const LaunchCfg &cfg, int mode,
+                                    cudaStream_t stream)
+{
+    return mode == EXT_MIXED ? launch_ext_mode<float, EXT_MIXED>(p, cfg, stream)
+                             : launch_ext_mode<float, EXT_FAST>(p, cfg, stream);
+}
+
+template <>
+cudaError_t launch_ext_trace<double>(const ExtParams<double> &p, const LaunchCfg &cfg, int mode,
+                                     cudaStream_t stream)
+{
+    if (mode != EXT_FAST)
+        return cudaErrorInvalidValue;
+    return launch_ext_mode<double, EXT_FAST>(p, cfg, stream);
+}
+
+template cudaError_t launch_ext_stage<float>(const void *, int, void *, int, int, int *, float *,
+                                             cudaStream_t);
+template cudaError_t launch_ext_stage<double>(const void *, int, void *, int, int, int *,
+                                              float *, cudaStream_t);
+
+} // namespace em

@@ -21,111 +21,10 @@
 // the IEEE sequence in both modes.
 #include "em_device.cuh"
 #include "em_internal.h"
+#include "em_math.cuh"
 
 namespace em {
 namespace {
-
-// ---- scalar IEEE operations without contraction --------------------------
-__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ float sqrt_rn(float a) { return __fsqrt_rn(a); }
-__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
-
-// MUFU reciprocal square root without the denormal-input fix-up sequence:
-// r2 is a sum of squares of coordinate differences and never denormal
-// unless the point sits on a charge, where both forms give inf.
-__device__ __forceinline__ float rsqrt_fast(float a)
-{
-    float d;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(d) : "f"(a));
-    return d;
-}
-__device__ __forceinline__ double rsqrt_fast(double a) { return rsqrt(a); }
-
-// ---- packed FP32 pairs (sm_100+ .f32x2): two charges per instruction ------
-typedef unsigned long long u64;
-__device__ __forceinline__ u64 f2_sub(u64 a, u64 b)
-{
-    u64 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ u64 f2_mul(u64 a, u64 b)
-{
-    u64 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ u64 f2_fma(u64 a, u64 b, u64 c)
-{
-    u64 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ u64 f2_pack(float lo, float hi)
-{
-    u64 d;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
-    return d;
-}
-__device__ __forceinline__ void f2_unpack(u64 v, float &lo, float &hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ u64 f2_rsqrt(u64 a)
-{
-    float lo, hi;
-    f2_unpack(a, lo, hi);
-    return f2_pack(rsqrt_fast(lo), rsqrt_fast(hi));
-}
-
-// Charge pair jp of a paired-layout tile {xa,xb,ya,yb,za,zb,qa,qb}:
-// a += q r / |r|^3 for both charges, lanes of the packed accumulators.
-__device__ __forceinline__ void pair2_fast(u64 px, u64 py, u64 pz, const ulonglong2 *tile,
-                                           int jp, u64 &ax, u64 &ay, u64 &az)
-{
-    const ulonglong2 A = tile[2 * jp], B = tile[2 * jp + 1];
-    const u64 dx = f2_sub(px, A.x), dy = f2_sub(py, A.y), dz = f2_sub(pz, B.x);
-    u64 r2 = f2_mul(dx, dx);
-    r2 = f2_fma(dy, dy, r2);
-    r2 = f2_fma(dz, dz, r2);
-    const u64 inv = f2_rsqrt(r2);
-    const u64 s = f2_mul(f2_mul(B.y, inv), f2_mul(inv, inv));
-    ax = f2_fma(s, dx, ax);
-    ay = f2_fma(s, dy, ay);
-    az = f2_fma(s, dz, az);
-}
-
-struct C4f {
-    float x, y, z, q;
-};
-struct C4d {
-    double x, y, z, q;
-};
-__device__ __forceinline__ C4f load_charge(const float4 *s, int j)
-{
-    const float4 c = s[j];
-    return {c.x, c.y, c.z, c.w};
-}
-__device__ __forceinline__ C4d load_charge(const ChargeD *s, int j)
-{
-    const double2 *p = reinterpret_cast<const double2 *>(s + j);
-    const double2 a = p[0], b = p[1];
-    return {a.x, a.y, b.x, b.y};
-}
-template <class T> struct C4;
-template <> struct C4<float> {
-    using type = C4f;
-};
-template <> struct C4<double> {
-    using type = C4d;
-};
 
 // One pair, fast form: a += q * r / |r|^3.
 template <class T, class C>
@@ -162,29 +61,6 @@ __device__ __forceinline__ void pair_exact(T px, T py, T pz, const C &c, T K, bo
     }
 }
 
-// Advance one vertex: the curvature rule of CPU_Implement.cpp:327-331
-// (r0 = curvature reference vector) or the fixed step of :89-90.
-template <class T>
-__device__ __forceinline__ void advance(T ex, T ey, T ez, T r0x, T r0y, T r0z, bool curvature,
-                                        T res, T &px, T &py, T &pz)
-{
-    const T k2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
-    T scale = res;
-    if (curvature) {
-        const T ix = sub_rn(ex, r0x), iy = sub_rn(ey, r0y), iz = sub_rn(ez, r0z);
-        const T cx = sub_rn(mul_rn(iy, r0z), mul_rn(iz, r0y));
-        const T cy = sub_rn(mul_rn(iz, r0x), mul_rn(ix, r0z));
-        const T cz = sub_rn(mul_rn(ix, r0y), mul_rn(iy, r0x));
-        const T c2 = add_rn(add_rn(mul_rn(cx, cx), mul_rn(cy, cy)), mul_rn(cz, cz));
-        const T kc = div_rn(sqrt_rn(c2), mul_rn(k2, sqrt_rn(k2)));
-        scale = mul_rn(add_rn(kc, T(1)), res);
-    }
-    const T s = mul_rn(scale, sqrt_rn(k2));
-    px = add_rn(px, div_rn(ex, s));
-    py = add_rn(py, div_rn(ey, s));
-    pz = add_rn(pz, div_rn(ez, s));
-}
-
 // Per-line field accumulator: scalar components, plus packed pairs for the
 // .f32x2 path (kept across charge tiles so tiling never changes the sum).
 template <class T> struct Acc {
@@ -198,12 +74,14 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
                                            T K, bool three_arg, Acc<T> &a)
 {
     if (ARITH == ARITH_FAST2) {
-        // charge pairs t, t+TPL, ... ; count is a multiple of 2*TPL
+        // charge pairs t, t+TPL, ... ; count is a multiple of 2*TPL; the tile
+        // holds its {xa,xb,ya,yb} plane, then its {za,zb,qa,qb} plane
         const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(tile);
+        const int G = count / 2;
         const u64 PX = f2_pack(px, px), PY = f2_pack(py, py), PZ = f2_pack(pz, pz);
 #pragma unroll 4
-        for (int jp = t; jp < count / 2; jp += TPL)
-            pair2_fast(PX, PY, PZ, tp, jp, a.X, a.Y, a.Z);
+        for (int jp = t; jp < G; jp += TPL)
+            pair2_fast(PX, PY, PZ, tp[jp], tp[G + jp], a.X, a.Y, a.Z);
     } else if (ARITH == ARITH_FAST) {
 #pragma unroll kUnroll
         for (int j = t; j < count; j += TPL)
@@ -230,15 +108,6 @@ __device__ __forceinline__ void acc_finish(Acc<T> &a)
     }
 }
 
-template <class T, int TPL>
-__device__ __forceinline__ T line_reduce(T v)
-{
-#pragma unroll
-    for (int o = TPL / 2; o >= 1; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 // KL lines per lane (fast scalar form only): one broadcast charge load feeds
 // KL independent pair chains, which doubles the work in flight per warp.
 template <class T, int TPL, int ARITH, int KL, class Rec>
@@ -246,10 +115,29 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
                                              const T *py, const T *pz, T K, bool three_arg,
                                              Acc<T> *a)
 {
-    if (KL == 1) {
+    if (ARITH == ARITH_FAST2 && KL > 1) {
+        // a charge pair (two LDS.128) feeds KL lines, two charges per
+        // packed instruction
+        const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(tile);
+        const int G = count / 2;
+        u64 PX[KL], PY[KL], PZ[KL];
+#pragma unroll
+        for (int k = 0; k < KL; ++k) {
+            PX[k] = f2_pack(px[k], px[k]);
+            PY[k] = f2_pack(py[k], py[k]);
+            PZ[k] = f2_pack(pz[k], pz[k]);
+        }
+#pragma unroll 2
+        for (int jp = t; jp < G; jp += TPL) {
+            const ulonglong2 A = tp[jp], B = tp[G + jp];
+#pragma unroll
+            for (int k = 0; k < KL; ++k)
+                pair2_fast(PX[k], PY[k], PZ[k], A, B, a[k].X, a[k].Y, a[k].Z);
+        }
+    } else if (KL == 1) {
         accumulate<T, TPL, ARITH>(tile, count, t, px[0], py[0], pz[0], K, three_arg, a[0]);
     } else {
-#pragma unroll 4
+#pragma unroll 8
         for (int j = t; j < count; j += TPL) {
             const auto c = load_charge(tile, j);
 #pragma unroll
@@ -352,7 +240,7 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
             break;
         long long line[KL];
         bool own[KL];
-        T px[KL], py[KL], pz[KL], r0x[KL], r0y[KL], r0z[KL];
+        T px[KL], py[KL], pz[KL];
 #pragma unroll
         for (int k = 0; k < KL; ++k) {
             // slot k of the warp's lines: consecutive lanes -> consecutive lines
@@ -364,11 +252,6 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                 py[k] = P.y[line[k]];
                 pz[k] = P.z[line[k]];
             }
-            // SSE rule: the curvature vector is the seed, loaded once
-            // (CPU_Implement.cpp:254-256) and never updated.
-            r0x[k] = px[k];
-            r0y[k] = py[k];
-            r0z[k] = pz[k];
         }
         for (int step = 1; step < P.total_steps; ++step) {
             Acc<T> acc[KL];
@@ -404,14 +287,19 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                     ay = mul_rn(ay, K);
                     az = mul_rn(az, K);
                 }
-                if (P.rule == RULE_GENERIC) {
-                    // prevVec = previous point (CPU_Implement.cpp:148-153)
-                    r0x[k] = px[k];
-                    r0y[k] = py[k];
-                    r0z[k] = pz[k];
+                // curvature vector: the seed for the SSE rule, loaded once in the
+                // reference (CPU_Implement.cpp:254-256) and never updated, here
+                // re-read from row 0 each step so it holds no registers during
+                // the pair loop; the previous point for the generic rule
+                // (CPU_Implement.cpp:148-153)
+                T r0x = px[k], r0y = py[k], r0z = pz[k];
+                if (P.rule == RULE_SSE && own[k]) {
+                    r0x = ld_seed(P.x + line[k]);
+                    r0y = ld_seed(P.y + line[k]);
+                    r0z = ld_seed(P.z + line[k]);
                 }
-                advance<T>(ax, ay, az, r0x[k], r0y[k], r0z[k], curvature, P.resolution, px[k],
-                           py[k], pz[k]);
+                advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k], py[k],
+                           pz[k]);
                 if (own[k] && t == 0) {
                     const size_t idx = (size_t)step * n + (size_t)line[k];
                     store_stream(P.x + idx, px[k]);
@@ -425,10 +313,12 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
 
 // Copies p charge records into the staged buffer of p_pad records, filling
 // [p, p_pad) with the pad record {1e15, 1e15, 1e15, 0} (its contribution is
-// exactly zero in every arithmetic), in plain {x,y,z,q} order or, when
-// `paired`, as pair-interleaved {xa,xb,ya,yb,za,zb,qa,qb} blocks.
+// exactly zero in every arithmetic), in plain {x,y,z,q} order (paired = 0)
+// or, for the packed form (1), in blocks of `block` records (one charge
+// tile): the block's {xa,xb,ya,yb} records, then its {za,zb,qa,qb} records,
+// so the lanes of a line read consecutive 16-B slots (no bank conflicts).
 template <class T>
-__global__ void stage_kernel(const T *raw, int p, T *staged, int p_pad, int paired)
+__global__ void stage_kernel(const T *raw, int p, T *staged, int p_pad, int paired, int block)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p_pad)
@@ -445,10 +335,14 @@ __global__ void stage_kernel(const T *raw, int p, T *staged, int p_pad, int pair
         for (int c = 0; c < 4; ++c)
             staged[4 * (size_t)i + c] = v[c];
     } else {
-        const size_t base = 8 * (size_t)(i >> 1);
-        const int h = i & 1;
-        for (int c = 0; c < 4; ++c)
-            staged[base + 2 * c + h] = v[c];
+        const int G = block / 2;      // pairs per block
+        const int jp = i >> 1, h = i & 1;
+        const size_t b0 = 4 * (size_t)(jp / G) * block; // block start (floats)
+        const size_t w = 4 * (size_t)(jp % G);
+        staged[b0 + w + h] = v[0];                    // A: {xa,xb,ya,yb}
+        staged[b0 + w + 2 + h] = v[1];
+        staged[b0 + 4 * (size_t)G + w + h] = v[2];    // B: {za,zb,qa,qb}
+        staged[b0 + 4 * (size_t)G + w + 2 + h] = v[3];
     }
 }
 
@@ -481,13 +375,20 @@ cudaError_t launch_fast(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaSt
                           : launch_one<T, TPL, ARITH_FAST, 1, 1024>(p, cfg, stream);
 }
 
+template <class T, int TPL>
+cudaError_t launch_packed(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
+{
+    return cfg.kl == 2 ? launch_one<T, TPL, ARITH_FAST2, 2, 1024>(p, cfg, stream)
+                       : launch_one<T, TPL, ARITH_FAST2, 1, 1024>(p, cfg, stream);
+}
+
 } // namespace
 
 template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream)
 {
-    if (cfg.kl != 1 && (cfg.kl != 2 || arith != ARITH_FAST))
+    if (cfg.kl != 1 && (cfg.kl != 2 || arith == ARITH_EXACT))
         return cudaErrorInvalidValue;
     if (arith == ARITH_EXACT) {
         if (cfg.tpl != 1)
@@ -498,10 +399,10 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, i
         if (sizeof(T) != 4)
             return cudaErrorInvalidValue;
         switch (cfg.tpl) {
-        case 1: return launch_one<T, 1, ARITH_FAST2, 1, 1024>(p, cfg, stream);
-        case 2: return launch_one<T, 2, ARITH_FAST2, 1, 1024>(p, cfg, stream);
-        case 4: return launch_one<T, 4, ARITH_FAST2, 1, 1024>(p, cfg, stream);
-        case 8: return launch_one<T, 8, ARITH_FAST2, 1, 1024>(p, cfg, stream);
+        case 1: return launch_packed<T, 1>(p, cfg, stream);
+        case 2: return launch_packed<T, 2>(p, cfg, stream);
+        case 4: return launch_packed<T, 4>(p, cfg, stream);
+        case 8: return launch_packed<T, 8>(p, cfg, stream);
         default: return cudaErrorInvalidValue;
         }
     }
@@ -516,12 +417,14 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, i
 
 template <class T>
 cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad, int paired,
-                                 cudaStream_t stream)
+                                 int block, cudaStream_t stream)
 {
     if (p_pad <= 0)
         return cudaSuccess;
+    if (paired && (block <= 0 || (block & 1) || p_pad % block))
+        return cudaErrorInvalidValue;
     stage_kernel<T><<<(p_pad + 127) / 128, 128, 0, stream>>>(
-        static_cast<const T *>(raw), p, static_cast<T *>(staged), p_pad, paired);
+        static_cast<const T *>(raw), p, static_cast<T *>(staged), p_pad, paired, block);
     count_launch(1);
     return cudaGetLastError();
 }
@@ -530,9 +433,9 @@ template cudaError_t launch_ref_trace<float>(const RefTraceParams<float> &, cons
                                              int, cudaStream_t);
 template cudaError_t launch_ref_trace<double>(const RefTraceParams<double> &,
                                               const LaunchCfg &, int, cudaStream_t);
-template cudaError_t launch_stage_charges<float>(const void *, int, void *, int, int,
+template cudaError_t launch_stage_charges<float>(const void *, int, void *, int, int, int,
                                                  cudaStream_t);
-template cudaError_t launch_stage_charges<double>(const void *, int, void *, int, int,
+template cudaError_t launch_stage_charges<double>(const void *, int, void *, int, int, int,
                                                   cudaStream_t);
 
 } // namespace em

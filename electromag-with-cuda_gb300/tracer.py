@@ -157,3 +157,100 @@ def field(points, charges, *, arith="fast", rule="sse", stream=None):
     if rc:
         raise _capi.EmError(rc, "em_field")
     return out.T
+
+
+_PREC = {"fp32": _capi.EM_PREC_FP32, "mixed": _capi.EM_PREC_MIXED}
+
+
+def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
+                steps_per_line=None, precision="fp32", want_field=False,
+                threads_per_line=0, warps_per_cta=0, tile_charges=0,
+                force_streamed=False, null_frac=0.0, stream=None):
+    """Extended method (seeded lines, termination, step limits).
+
+    seeds (n, 3), charges (p, 4): numpy arrays (host entry point) or CUDA
+    torch tensors (device entry point, current stream).  precision: "fp32",
+    "mixed" (FP32 pairs, FP64 positions and near-null fields) or "fp64".
+    Returns a dict with vertices (3, max_steps, n), len (n,), cls (n,),
+    field (3, max_steps, n) when want_field, and perf.
+    """
+    import ctypes
+    lib = _capi.load()
+    f64 = precision == "fp64"
+    o = _capi.EmOptions()
+    o.precision = _capi.EM_PREC_FP32 if f64 else _PREC[precision]
+    o.threads_per_line = threads_per_line
+    o.warps_per_cta = warps_per_cta
+    o.tile_charges = tile_charges
+    o.force_streamed = int(bool(force_streamed))
+    o.null_frac = null_frac
+    perf = _capi.EmPerf()
+    fn = lib.em_trace_lines_f64 if f64 else lib.em_trace_lines_f32
+    if _is_torch(seeds):
+        import torch
+        dt = torch.float64 if f64 else torch.float32
+        n = seeds.shape[0]
+        dev = seeds.device
+        V = torch.empty((3, max_steps, n), dtype=dt, device=dev)
+        V[:, 0, :] = seeds.T.to(dt)
+        ln = torch.zeros(n, dtype=torch.int32, device=dev)
+        cl = torch.zeros(n, dtype=torch.int32, device=dev)
+        F = (torch.empty((3, max_steps, n), dtype=dt, device=dev)
+             if want_field else None)
+        ch = charges.to(dt).contiguous()
+        spl = (steps_per_line.to(torch.int32).contiguous()
+               if steps_per_line is not None else None)
+        o.device_ptrs = 1
+        o.stream = (stream if stream is not None else
+                    torch.cuda.current_stream(dev).cuda_stream)
+        rc = fn(V[0].data_ptr(), V[1].data_ptr(), V[2].data_ptr(), n,
+                max_steps, spl.data_ptr() if spl is not None else None,
+                ch.data_ptr(), ch.numel() // 4, resolution, term_radius,
+                ln.data_ptr(), cl.data_ptr(),
+                F[0].data_ptr() if F is not None else None,
+                F[1].data_ptr() if F is not None else None,
+                F[2].data_ptr() if F is not None else None,
+                ctypes_byref(o), ctypes_byref(perf))
+    else:
+        dt = np.float64 if f64 else np.float32
+        seeds = np.asarray(seeds)
+        n = seeds.shape[0]
+        V = np.zeros((3, max_steps, n), dt)
+        V[:, 0, :] = seeds.T
+        ln = np.zeros(n, np.int32)
+        cl = np.zeros(n, np.int32)
+        F = np.zeros((3, max_steps, n), dt) if want_field else None
+        ch = np.ascontiguousarray(charges, dt)
+        spl = (np.ascontiguousarray(steps_per_line, np.int32)
+               if steps_per_line is not None else None)
+        rc = fn(V[0].ctypes.data, V[1].ctypes.data, V[2].ctypes.data, n,
+                max_steps, spl.ctypes.data if spl is not None else None,
+                ch.ctypes.data, ch.size // 4, resolution, term_radius,
+                ln.ctypes.data, cl.ctypes.data,
+                F[0].ctypes.data if F is not None else None,
+                F[1].ctypes.data if F is not None else None,
+                F[2].ctypes.data if F is not None else None,
+                ctypes_byref(o), ctypes_byref(perf))
+    if rc:
+        raise _capi.EmError(rc, "em_trace_lines")
+    out = dict(vertices=V, len=ln, cls=cl, perf=perf)
+    if want_field:
+        out["field"] = F
+    return out
+
+
+def seed_fibonacci(charges, lines_per_charge, radius=1.0):
+    """Seeds around every positive charge (em_seed_fibonacci_f32); (m, 3)."""
+    import ctypes
+    lib = _capi.load()
+    ch = np.ascontiguousarray(charges, np.float32)
+    cap = int((ch[:, 3] > 0).sum()) * int(lines_per_charge)
+    out = np.zeros((3, max(cap, 1)), np.float32)
+    cnt = ctypes.c_size_t()
+    rc = lib.em_seed_fibonacci_f32(ch.ctypes.data, len(ch), lines_per_charge,
+                                   radius, out[0].ctypes.data,
+                                   out[1].ctypes.data, out[2].ctypes.data,
+                                   cap, ctypes.addressof(cnt))
+    if rc:
+        raise _capi.EmError(rc, "em_seed_fibonacci_f32")
+    return out[:, : cnt.value].T.copy()

@@ -74,6 +74,7 @@ typedef struct em_perf {
     volatile double progress; /* 0 before the call, 1.0 when complete        */
     double pairs;        /* pair interactions evaluated                      */
     double wall_time;    /* seconds of the whole call (copies included)      */
+    double fp64_refines; /* vertices whose field was redone in FP64 (mixed)  */
 } em_perf;
 
 /* Options for the _ex entry points.  Zero-initialise and set what you need. */
@@ -90,8 +91,23 @@ typedef struct em_options {
     int tile_charges;     /* 0: automatic; streamed-charge tile size         */
     int force_streamed;   /* 1: stream charge tiles even if they fit          */
     int pack;             /* EM_PACK_*: pair loop form for fast FP32         */
-    int lines_per_thread; /* 0: automatic; 1 or 2 (fast scalar form only)    */
+    int lines_per_thread; /* 0: automatic; 1 or 2 (fast arithmetic only)     */
+    int precision;        /* em_trace_lines_f32: EM_PREC_FP32 or EM_PREC_MIXED */
+    double null_frac;     /* mixed: FP64 re-evaluation where |E| is below this
+                             fraction of the largest single contribution
+                             (0: 1e-4)                                       */
 } em_options;
+
+/* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
+#define EM_PREC_FP32 0    /* FP32 pairs and positions                        */
+#define EM_PREC_MIXED 1   /* FP32 pairs with a Newton-corrected inv^3,
+                             compensated sums, FP64 positions, FP64 field
+                             near nulls                                      */
+
+/* ---- termination classes of the extended tracer --------------------------- */
+#define EM_TERM_STEPS 0   /* reached its step limit                          */
+#define EM_TERM_CHARGE 1  /* came within term_radius of a negative charge    */
+#define EM_TERM_NULL 2    /* zero or non-finite field / step                 */
 
 /* ---- pair loop form (fast FP32 only) -------------------------------------- */
 #define EM_PACK_AUTO 0    /* library's choice                                */
@@ -140,6 +156,46 @@ EM_API int em_calc_field_noalloc_f32(float *x, float *y, float *z, size_t n,
                                      size_t total_steps, const float *charges,
                                      size_t p, float resolution,
                                      int use_curvature, void *stream);
+
+/* Extended method: field lines seeded around charges (em_seed_fibonacci_*),
+ * traced with the reference's stepping rule (CPU_Implement.cpp:322-338:
+ * curvature against the line's seed) until, for s = 1.., the field at
+ * vertex s-1 is evaluated and that vertex lies strictly within term_radius
+ * of a negative charge (EM_TERM_CHARGE), the field or the step is zero or
+ * non-finite (EM_TERM_NULL), or the line has max_steps vertices (or
+ * steps_per_line[line], when given) (EM_TERM_STEPS).  The reference stops
+ * only at the step limit; seeding and termination are additions.
+ * Layout as the reference's: x, y, z of n*max_steps, vertex (line, s) at
+ * s*n + line, row 0 = seeds.  len[line] = vertices written (seed included),
+ * cls[line] = EM_TERM_*; rows at and after len[line] are unspecified.
+ * ex, ey, ez (optional, n*max_steps): the field evaluated at vertex s, at
+ * row s, for every evaluated vertex.  opt->precision selects FP32 or mixed
+ * precision (_f32); _f64 runs FP64 throughout.  Host pointers unless
+ * opt->device_ptrs.  perf->pairs counts field evaluations x p. */
+EM_API int em_trace_lines_f32(float *x, float *y, float *z, size_t n,
+                              size_t max_steps, const int32_t *steps_per_line,
+                              const float *charges, size_t p, float resolution,
+                              float term_radius, int32_t *len, int32_t *cls,
+                              float *ex, float *ey, float *ez,
+                              const em_options *opt, em_perf *perf);
+EM_API int em_trace_lines_f64(double *x, double *y, double *z, size_t n,
+                              size_t max_steps, const int32_t *steps_per_line,
+                              const double *charges, size_t p,
+                              double resolution, double term_radius,
+                              int32_t *len, int32_t *cls, double *ex,
+                              double *ey, double *ez, const em_options *opt,
+                              em_perf *perf);
+
+/* Seeds on a sphere of `radius` around every positive charge (q > 0), in
+ * charge order: lines_per_charge golden-angle spiral directions
+ * (z_i = 1 - (2i+1)/L, phi_i = i * pi (3 - sqrt 5)).  Writes at most cap
+ * seeds to sx, sy, sz (host arrays) and their number to *count.  The
+ * reference seeds from a grid or random points ("Electromag utils.h":29-70);
+ * this seeding is the extended method's. */
+EM_API int em_seed_fibonacci_f32(const float *charges, size_t p,
+                                 size_t lines_per_charge, float radius,
+                                 float *sx, float *sy, float *sz, size_t cap,
+                                 size_t *count);
 
 /* Field at m points, no stepping: E_i = sum_j PartField(charge_j, point_i)
  * summed in charge order (include/Electrostatics.h:38-60 as

@@ -142,7 +142,7 @@ def first_approach(v, ch, radius):
 
 
 @pytest.mark.parametrize("pack,kl", [("scalar", 1), ("scalar", 2),
-                                     ("pairs", 1)])
+                                     ("pairs", 1), ("pairs", 2)])
 def test_fast_vertices_within_1e4_first_500_steps(em, gpu, orc, cpu_config,
                                                   pack, kl):
     ch, seeds, steps = cpu_config
@@ -168,7 +168,7 @@ def test_fast_vertices_within_1e4_first_500_steps(em, gpu, orc, cpu_config,
 
 
 @pytest.mark.parametrize("pack,kl", [("scalar", 1), ("scalar", 2),
-                                     ("pairs", 1)])
+                                     ("pairs", 1), ("pairs", 2)])
 @pytest.mark.parametrize("tpl", [1, 2, 4, 8])
 def test_fast_threads_per_line_variants_agree(em, gpu, golden, tpl, pack, kl):
     name = "curv_f32"
@@ -181,7 +181,7 @@ def test_fast_threads_per_line_variants_agree(em, gpu, golden, tpl, pack, kl):
 
 
 @pytest.mark.parametrize("pack,kl", [("scalar", 1), ("scalar", 2),
-                                     ("pairs", 1)])
+                                     ("pairs", 1), ("pairs", 2)])
 @pytest.mark.parametrize("tpl", [1, 4])
 def test_fast_streamed_equals_resident_bitwise(em, gpu, cpu_config, tpl, pack,
                                                kl):
