@@ -70,6 +70,8 @@ _SIGNATURES = {
     "em_trace_lines_f64": (I, [P, P, P, S, S, P, P, S, D, D, P, P, P, P, P,
                                P, P]),
     "em_seed_fibonacci_f32": (I, [P, S, S, F, P, P, P, S, P]),
+    "em_adjoint_f32": (I, [P, P, P, S, S, P, S, F, I, P, P, P, P, P, P, P,
+                           P]),
     "em_field_f32": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_field_f64": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_fp32_peak_tflops": (I, [P, P]),

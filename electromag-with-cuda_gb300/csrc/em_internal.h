@@ -92,6 +92,28 @@ template <class T>
 cudaError_t launch_ext_trace(const ExtParams<T> &p, const struct LaunchCfg &cfg, int mode,
                              cudaStream_t stream);
 
+// Adjoint of the frozen-step map (em_adjoint.cu).
+struct AdjParams {
+    const float *x, *y, *z;    // forward vertices, n*rows
+    const float *tx, *ty, *tz; // targets, n*rows
+    const void *charges;       // staged plain records, p_pad (padded)
+    const float *raw;          // the caller's p records
+    int p, p_pad;
+    long long n;
+    int rows, seg;
+    float resolution;
+    int curvature;
+    float *abar;               // 3n: dL/dv of the current row (x, y, z blocks)
+    float *rec;                // 6 blocks of rec_stride floats: v, mu per record
+    size_t rec_stride;         // >= seg * n
+    double *gpart;             // slices * p * 4 partial sums
+    int slices;
+    int *err;
+};
+int adjoint_charge_blocks(int p);
+cudaError_t launch_adjoint_backward(const AdjParams &P, int nsm, size_t smem, double *loss,
+                                    double *grad, cudaStream_t stream);
+
 struct LaunchCfg {
     int tpl;     // threads per line (1, 2, 4, 8)
     int kl;      // lines per lane (1, 2; 2 only for the fast forms)

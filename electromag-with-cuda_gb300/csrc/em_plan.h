@@ -30,8 +30,10 @@ struct DevCtx {
     size_t lines_cap = 0;
     void *errbuf = nullptr;
     size_t errbuf_cap = 0;
-    void *scratch = nullptr; // field-at-points staging
+    void *scratch = nullptr; // field-at-points / extended / adjoint staging
     size_t scratch_cap = 0;
+    void *adj = nullptr;     // adjoint workspace
+    size_t adj_cap = 0;
     int *err = nullptr;
 };
 

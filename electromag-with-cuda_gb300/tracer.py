@@ -254,3 +254,60 @@ def seed_fibonacci(charges, lines_per_charge, radius=1.0):
     if rc:
         raise _capi.EmError(rc, "em_seed_fibonacci_f32")
     return out[:, : cnt.value].T.copy()
+
+
+def adjoint(seeds, charges, rows, targets, resolution=1.0, use_curvature=True):
+    """Loss sum |v - t|^2 over the traced vertices and its gradient with
+    respect to the charges (em_adjoint_f32, frozen step lengths).
+
+    seeds (n, 3), charges (p, 4), targets (3, rows, n): numpy arrays.
+    Returns dict(loss, grad (p, 4) float64 [dx, dy, dz, dq], vertices
+    (3, rows, n), fwd_time, bwd_time)."""
+    lib = _capi.load()
+    seeds = np.asarray(seeds, np.float32)
+    n = seeds.shape[0]
+    V = np.zeros((3, rows, n), np.float32)
+    V[:, 0, :] = seeds.T
+    T = np.ascontiguousarray(targets, np.float32)
+    ch = np.ascontiguousarray(charges, np.float32)
+    p = ch.shape[0]
+    loss = np.zeros(1, np.float64)
+    grad = np.zeros((p, 4), np.float64)
+    fwd, bwd = _capi.EmPerf(), _capi.EmPerf()
+    rc = lib.em_adjoint_f32(V[0].ctypes.data, V[1].ctypes.data,
+                            V[2].ctypes.data, n, rows, ch.ctypes.data, p,
+                            resolution, int(bool(use_curvature)),
+                            T[0].ctypes.data, T[1].ctypes.data,
+                            T[2].ctypes.data, loss.ctypes.data,
+                            grad.ctypes.data, None, ctypes_byref(fwd),
+                            ctypes_byref(bwd))
+    if rc:
+        raise _capi.EmError(rc, "em_adjoint_f32")
+    return dict(loss=float(loss[0]), grad=grad, vertices=V,
+                fwd_time=fwd.time, bwd_time=bwd.time)
+
+
+def trace_loss_function():
+    """torch.autograd.Function: loss = TraceLoss.apply(charges, seeds, rows,
+    targets, resolution, use_curvature); charges (p, 4) CPU tensor.  The
+    forward runs the tracer and its adjoint together; backward scales the
+    stored gradient."""
+    import torch
+
+    class TraceLoss(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, charges, seeds, rows, targets, resolution=1.0,
+                    use_curvature=True):
+            out = adjoint(seeds.detach().cpu().numpy(),
+                          charges.detach().cpu().numpy(), rows,
+                          targets.detach().cpu().numpy(), resolution,
+                          use_curvature)
+            ctx.save_for_backward(torch.from_numpy(out["grad"]).to(charges))
+            return charges.new_tensor(out["loss"])
+
+        @staticmethod
+        def backward(ctx, gout):
+            (g,) = ctx.saved_tensors
+            return gout * g, None, None, None, None, None
+
+    return TraceLoss

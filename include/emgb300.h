@@ -186,6 +186,25 @@ EM_API int em_trace_lines_f64(double *x, double *y, double *z, size_t n,
                               double *ey, double *ez, const em_options *opt,
                               em_perf *perf);
 
+/* Gradients of a vertex loss through the tracer (no counterpart in the
+ * reference).  Runs the forward trace (fast FP32, the reference rule:
+ * curvature against the seed when use_curvature, else the fixed step) on
+ * x, y, z (row 0 = seeds in, rows 1..rows-1 written), then the adjoint of
+ * the discrete map v_{s+1} = v_s + lam_s E_s/|E_s| with the step lengths
+ * lam_s = 1/((k_s+1) res) held at their forward values:
+ *   *loss = sum over lines and rows of |v - t|^2 (targets tx, ty, tz),
+ *   grad[4j+c] = dL/d(charge j component c), c = x, y, z, q (FP64).
+ * The backward recomputes the fields from the stored vertices in segments
+ * of 64 rows.  Charges must fit in shared memory (p <= 14000, else
+ * EM_ERR_TOO_LARGE).  fwd / bwd (optional) receive the forward and the
+ * backward device times (time) and pair counts.  Host pointers unless
+ * opt->device_ptrs. */
+EM_API int em_adjoint_f32(float *x, float *y, float *z, size_t n, size_t rows,
+                          const float *charges, size_t p, float resolution,
+                          int use_curvature, const float *tx, const float *ty,
+                          const float *tz, double *loss, double *grad,
+                          const em_options *opt, em_perf *fwd, em_perf *bwd);
+
 /* Seeds on a sphere of `radius` around every positive charge (q > 0), in
  * charge order: lines_per_charge golden-angle spiral directions
  * (z_i = 1 - (2i+1)/L, phi_i = i * pi (3 - sqrt 5)).  Writes at most cap

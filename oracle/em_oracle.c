@@ -348,3 +348,169 @@ size_t orc_seed_fibonacci_f64(const double *charges, size_t p,
     }
     return w;
 }
+
+/* ---------------------------------------------------------------------------
+ * Adjoint checks: the frozen-step map, its complex-step derivative and its
+ * discrete adjoint, all in FP64 (test infrastructure).
+ */
+#include <complex.h>
+#include <stdlib.h>
+
+/* E' = sum_j q_j r / |r|^3 (the Coulomb constant factored out). */
+static void field_prime(const double *ch, size_t p, double x, double y,
+                        double z, double *e)
+{
+    double ax = 0, ay = 0, az = 0;
+    for (size_t j = 0; j < p; ++j) {
+        const double rx = x - ch[4 * j], ry = y - ch[4 * j + 1],
+                     rz = z - ch[4 * j + 2], q = ch[4 * j + 3];
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double s = q / (r2 * sqrt(r2));
+        ax += s * rx;
+        ay += s * ry;
+        az += s * rz;
+    }
+    e[0] = ax;
+    e[1] = ay;
+    e[2] = az;
+}
+
+/* lam = 1/((k+1) res) with k = |(E - P0) x P0| / |E|^3, E = K E'. */
+static double frozen_lambda(const double *ep, const double *p0, double res)
+{
+    const double K = ORC_ELECTRO_K;
+    const double ex = K * ep[0], ey = K * ep[1], ez = K * ep[2];
+    const double k2 = ex * ex + ey * ey + ez * ez;
+    const double ix = ex - p0[0], iy = ey - p0[1], iz = ez - p0[2];
+    const double cx = iy * p0[2] - iz * p0[1], cy = iz * p0[0] - ix * p0[2],
+                 cz = ix * p0[1] - iy * p0[0];
+    const double kc = sqrt(cx * cx + cy * cy + cz * cz) / (k2 * sqrt(k2));
+    return 1.0 / ((kc + 1.0) * res);
+}
+
+double orc_frozen_loss_f64(const double *charges, size_t p, const double *sx,
+                           const double *sy, const double *sz, size_t n,
+                           size_t S, double res, const double *tx,
+                           const double *ty, const double *tz,
+                           const double *lam_in, double *lam_out, double *vx,
+                           double *vy, double *vz)
+{
+    double L = 0;
+    for (size_t l = 0; l < n; ++l) {
+        double v[3] = {sx[l], sy[l], sz[l]};
+        const double p0[3] = {sx[l], sy[l], sz[l]};
+        for (size_t s = 0; s < S; ++s) {
+            const size_t i = s * n + l;
+            const double dx = v[0] - tx[i], dy = v[1] - ty[i], dz = v[2] - tz[i];
+            L += dx * dx + dy * dy + dz * dz;
+            if (vx) {
+                vx[i] = v[0];
+                vy[i] = v[1];
+                vz[i] = v[2];
+            }
+            if (s + 1 == S)
+                break;
+            double e[3];
+            field_prime(charges, p, v[0], v[1], v[2], e);
+            const double lam = lam_in ? lam_in[i] : frozen_lambda(e, p0, res);
+            if (lam_out)
+                lam_out[i] = lam;
+            const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+            for (int c = 0; c < 3; ++c)
+                v[c] += lam * e[c] / en;
+        }
+    }
+    return L;
+}
+
+double orc_frozen_loss_cs_f64(const double *charges, size_t p, const double *sx,
+                              const double *sy, const double *sz, size_t n,
+                              size_t S, double res, const double *tx,
+                              const double *ty, const double *tz,
+                              const double *lam_in, size_t j, int c, double h)
+{
+    (void)res;
+    double complex *ch = malloc(sizeof(double complex) * 4 * p);
+    for (size_t k = 0; k < 4 * p; ++k)
+        ch[k] = charges[k];
+    ch[4 * j + (size_t)c] += I * h;
+    double complex L = 0;
+    for (size_t l = 0; l < n; ++l) {
+        double complex v[3] = {sx[l], sy[l], sz[l]};
+        for (size_t s = 0; s < S; ++s) {
+            const size_t i = s * n + l;
+            const double complex dx = v[0] - tx[i], dy = v[1] - ty[i],
+                                 dz = v[2] - tz[i];
+            L += dx * dx + dy * dy + dz * dz;
+            if (s + 1 == S)
+                break;
+            double complex e[3] = {0, 0, 0};
+            for (size_t k = 0; k < p; ++k) {
+                const double complex rx = v[0] - ch[4 * k], ry = v[1] - ch[4 * k + 1],
+                                     rz = v[2] - ch[4 * k + 2];
+                const double complex r2 = rx * rx + ry * ry + rz * rz;
+                const double complex sc = ch[4 * k + 3] / (r2 * csqrt(r2));
+                e[0] += sc * rx;
+                e[1] += sc * ry;
+                e[2] += sc * rz;
+            }
+            const double complex en = csqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+            for (int d = 0; d < 3; ++d)
+                v[d] += lam_in[i] * e[d] / en;
+        }
+    }
+    free(ch);
+    return cimag(L) / h;
+}
+
+double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
+                           const double *sy, const double *sz, size_t n,
+                           size_t S, double res, const double *tx,
+                           const double *ty, const double *tz,
+                           const double *lam_in, double *grad)
+{
+    double *vx = malloc(sizeof(double) * S * n), *vy = malloc(sizeof(double) * S * n),
+           *vz = malloc(sizeof(double) * S * n);
+    const double L = orc_frozen_loss_f64(charges, p, sx, sy, sz, n, S, res, tx, ty,
+                                         tz, lam_in, NULL, vx, vy, vz);
+    for (size_t k = 0; k < 4 * p; ++k)
+        grad[k] = 0;
+    for (size_t l = 0; l < n; ++l) {
+        const size_t last = (S - 1) * n + l;
+        double a[3] = {2 * (vx[last] - tx[last]), 2 * (vy[last] - ty[last]),
+                       2 * (vz[last] - tz[last])};
+        for (size_t s = S - 1; s-- > 0;) {
+            const size_t i = s * n + l;
+            const double v[3] = {vx[i], vy[i], vz[i]};
+            double e[3];
+            field_prime(charges, p, v[0], v[1], v[2], e);
+            const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+            const double u[3] = {e[0] / en, e[1] / en, e[2] / en};
+            const double ua = u[0] * a[0] + u[1] * a[1] + u[2] * a[2];
+            double mu[3];
+            for (int c = 0; c < 3; ++c)
+                mu[c] = lam_in[i] * (a[c] - u[c] * ua) / en;
+            double jm[3] = {0, 0, 0};
+            for (size_t j = 0; j < p; ++j) {
+                const double r[3] = {v[0] - charges[4 * j], v[1] - charges[4 * j + 1],
+                                     v[2] - charges[4 * j + 2]};
+                const double q = charges[4 * j + 3];
+                const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+                const double i3 = 1.0 / (r2 * sqrt(r2));
+                const double d = r[0] * mu[0] + r[1] * mu[1] + r[2] * mu[2];
+                for (int c = 0; c < 3; ++c) {
+                    const double g = mu[c] * i3 - 3.0 * r[c] * d * i3 / r2;
+                    jm[c] += q * g;
+                    grad[4 * j + (size_t)c] -= q * g;
+                }
+                grad[4 * j + 3] += d * i3;
+            }
+            for (int c = 0; c < 3; ++c)
+                a[c] = 2 * (v[c] - (c == 0 ? tx[i] : c == 1 ? ty[i] : tz[i])) + a[c] + jm[c];
+        }
+    }
+    free(vx);
+    free(vy);
+    free(vz);
+    return L;
+}

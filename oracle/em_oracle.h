@@ -103,3 +103,40 @@ size_t orc_seed_fibonacci_f64(const double *charges, size_t p,
 }
 #endif
 #endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/*
+ * Adjoint checks (FP64).  The frozen-step map of the reference rule:
+ *   v_{s+1} = v_s + lam_s * E(v_s) / |E(v_s)|,
+ *   lam_s = 1 / ((k_s + 1) * res), k_s the curvature of CPU_Implement.cpp:
+ *   327-329 against the seed, computed on the unperturbed trajectory.
+ * Loss L = sum over lines and rows s = 0..S-1 of |v_s - t_s|^2.
+ * Layout: seeds sx/sy/sz (n), targets and vertices s*n + line (S rows).
+ * lam (n*(S-1), s*n + line): written when lam_out is non-null; the map
+ * uses lam_in when it is non-null, else its own lam.
+ */
+double orc_frozen_loss_f64(const double *charges, size_t p, const double *sx,
+                           const double *sy, const double *sz, size_t n,
+                           size_t S, double res, const double *tx,
+                           const double *ty, const double *tz,
+                           const double *lam_in, double *lam_out, double *vx,
+                           double *vy, double *vz);
+/* Complex-step derivative of the frozen loss (lam_in required) with respect
+ * to charge j's component c (0..2 position, 3 magnitude): Im L(x + ih) / h. */
+double orc_frozen_loss_cs_f64(const double *charges, size_t p, const double *sx,
+                              const double *sy, const double *sz, size_t n,
+                              size_t S, double res, const double *tx,
+                              const double *ty, const double *tz,
+                              const double *lam_in, size_t j, int c, double h);
+/* Discrete adjoint of the frozen map in FP64: grad[4j+c] = dL/d(charge j,
+ * component c) (c: x, y, z, q).  Returns L. */
+double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
+                           const double *sy, const double *sz, size_t n,
+                           size_t S, double res, const double *tx,
+                           const double *ty, const double *tz,
+                           const double *lam_in, double *grad);
+#ifdef __cplusplus
+}
+#endif

@@ -42,6 +42,16 @@ def load():
         lib.orc_seed_fibonacci_f64.argtypes = [P, S, S, ctypes.c_double, P, P,
                                                P, S]
         lib.orc_seed_fibonacci_f64.restype = S
+        D = ctypes.c_double
+        lib.orc_frozen_loss_f64.restype = D
+        lib.orc_frozen_loss_f64.argtypes = [P, S, P, P, P, S, S, D, P, P, P,
+                                            P, P, P, P, P]
+        lib.orc_frozen_loss_cs_f64.restype = D
+        lib.orc_frozen_loss_cs_f64.argtypes = [P, S, P, P, P, S, S, D, P, P,
+                                               P, P, S, I, D]
+        lib.orc_frozen_grad_f64.restype = D
+        lib.orc_frozen_grad_f64.argtypes = [P, S, P, P, P, S, S, D, P, P, P,
+                                            P, P]
         _lib = lib
     return _lib
 
@@ -109,3 +119,49 @@ def trace_lines_f64(charges, seeds, max_steps, resolution=1.0,
     if rc:
         raise RuntimeError(f"orc_trace_lines_f64 returned {rc}")
     return v, ln, cl
+
+
+class Frozen:
+    """FP64 frozen-step map of the reference rule (adjoint checks): the
+    step lengths come from the unperturbed trajectory of `charges`."""
+
+    def __init__(self, charges, seeds, rows, targets, resolution=1.0):
+        self.lib = load()
+        self.ch = np.ascontiguousarray(charges, np.float64)
+        seeds = np.asarray(seeds, np.float64)
+        self.s = [np.ascontiguousarray(seeds[:, c]) for c in range(3)]
+        self.n, self.S, self.res = len(seeds), rows, resolution
+        self.t = [np.ascontiguousarray(np.asarray(targets[c], np.float64)
+                                       .reshape(-1)) for c in range(3)]
+        self.lam = np.zeros((rows - 1) * self.n)
+        self.V = [np.zeros(rows * self.n) for _ in range(3)]
+        self.L = self.lib.orc_frozen_loss_f64(
+            _p(self.ch), len(self.ch), *map(_p, self.s), self.n, rows,
+            resolution, *map(_p, self.t), None, _p(self.lam),
+            *map(_p, self.V))
+
+    def loss(self, charges):
+        ch = np.ascontiguousarray(charges, np.float64)
+        return self.lib.orc_frozen_loss_f64(
+            _p(ch), len(ch), *map(_p, self.s), self.n, self.S, self.res,
+            *map(_p, self.t), _p(self.lam), None, None, None, None)
+
+    def grad(self):
+        g = np.zeros(self.ch.size)
+        self.lib.orc_frozen_grad_f64(_p(self.ch), len(self.ch),
+                                     *map(_p, self.s), self.n, self.S,
+                                     self.res, *map(_p, self.t),
+                                     _p(self.lam), _p(g))
+        return g.reshape(-1, 4)
+
+    def complex_step(self, j, c, h=1e-30):
+        return self.lib.orc_frozen_loss_cs_f64(
+            _p(self.ch), len(self.ch), *map(_p, self.s), self.n, self.S,
+            self.res, *map(_p, self.t), _p(self.lam), j, c, h)
+
+    def central(self, j, c, h=1e-3):
+        cp = self.ch.copy()
+        cm = self.ch.copy()
+        cp[j, c] += h
+        cm[j, c] -= h
+        return (self.loss(cp) - self.loss(cm)) / (2 * h)

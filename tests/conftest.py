@@ -75,3 +75,25 @@ def lines_from(seeds, steps, dtype):
         a[:n] = seeds[:, c]
         out.append(a)
     return out
+
+
+@pytest.fixture(scope="session")
+def adjoint_case(orc):
+    """24 charges in [-10,10]^3, 48 lines seeded 35..45 from the origin
+    (well conditioned: no line comes near a charge in 24 rows)."""
+    rng = np.random.default_rng(42)
+    p, n, rows = 24, 48, 24
+    ch = np.zeros((p, 4))
+    ch[:, :3] = rng.uniform(-10, 10, (p, 3))
+    ch[:, 3] = rng.uniform(1, 10, p) * rng.choice([-1, 1], p)
+    d = rng.normal(size=(n, 3))
+    seeds = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(35, 45, (n, 1))
+    ch = ch.astype(np.float32).astype(np.float64)
+    seeds = seeds.astype(np.float32).astype(np.float64)
+    fz = orc.Frozen(ch, seeds, rows, np.zeros((3, rows, n)))
+    V = np.stack([v.reshape(rows, n) for v in fz.V])
+    targets = (V + rng.normal(0, 0.1, V.shape)).astype(np.float32)
+    fz = orc.Frozen(ch, seeds, rows, targets.astype(np.float64))
+    return ch, seeds, rows, targets, fz
+
+
