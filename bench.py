@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--kl", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--pack", default="auto")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the extended / precision / adjoint blocks")
     return ap.parse_args()
 
 
@@ -263,6 +265,10 @@ def main():
     if not args.no_e2e:
         e2e = run_e2e(em, torch, dist, ch, seeds, rows, args, world)
 
+    extras = {}
+    if not args.no_extras:
+        extras = run_extras(em, torch, dev, args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -298,10 +304,128 @@ def main():
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    line.update(extras)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def field_errors(em, torch, ch, V, F, ln, samples, seed):
+    """Relative field error of a run's stored fields against the FP64 field
+    (em_field_f64, the reference's double sequence) at sampled vertices."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    lnh = ln.cpu().numpy()
+    rows_ok = np.maximum(lnh - 1, 0)  # rows with a field that led to a step
+    lines = np.nonzero(rows_ok)[0]
+    if len(lines) == 0:
+        return None
+    li = g.choice(lines, samples)
+    ri = (g.random(samples) * rows_ok[li]).astype(np.int64)
+    li_t = torch.from_numpy(li).to(V.device)
+    ri_t = torch.from_numpy(ri).to(V.device)
+    pts = V[:, ri_t, li_t].double()                 # (3, m)
+    got = F[:, ri_t, li_t].double()
+    ref = em.field(pts.contiguous(), ch.double().contiguous(), arith="exact")
+    err = (got - ref).norm(dim=0) / ref.norm(dim=0)
+    e = err.cpu().numpy()
+    return {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
+            "p999": float(np.quantile(e, 0.999)), "max": float(e.max()),
+            "frac_le_1e-6": float((e <= 1e-6).mean()), "samples": int(samples)}
+
+
+def traced(em, torch, ch, seeds, steps, term, precision, want_field,
+           null_frac=0.0):
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    em.trace_lines(seeds.to(dt), ch.to(dt), min(steps, 8), 1.0, term,
+                   precision=precision, null_frac=null_frac)  # warm-up
+    torch.cuda.synchronize()
+    out = em.trace_lines(seeds.to(dt), ch.to(dt), steps, 1.0, term,
+                         precision=precision, want_field=want_field,
+                         null_frac=null_frac)
+    torch.cuda.synchronize()
+    perf = out["perf"]
+    out["gpairs"] = perf.pairs / perf.time / 1e9 if perf.time > 0 else 0.0
+    return out
+
+
+def precision_block(em, torch, dev, name, steps, seed, samples, with_ratio):
+    """FP32 / mixed / FP64 runs of the extended method on one workload, with
+    throughput and field error vs FP64."""
+    ch_np, seeds_np, _ = em.workloads.make(name, seed=seed)
+    ch = torch.from_numpy(np.ascontiguousarray(ch_np, np.float32)).to(dev)
+    seeds = torch.from_numpy(seeds_np.astype(np.float32)).to(dev)
+    blk = {"workload": name, "lines": int(len(seeds_np)),
+           "charges": int(len(ch_np)), "max_rows": steps,
+           "term_radius": 0.5}
+    for prec, nf in (("fp32", 0.0), ("mixed", 0.0), ("mixed_nf0.05", 0.05),
+                     ("fp64", 0.0)):
+        p = "mixed" if prec.startswith("mixed") else prec
+        out = traced(em, torch, ch, seeds, steps, 0.5, p, True, nf)
+        ln = out["len"]
+        cls = np.bincount(out["cls"].cpu().numpy(), minlength=3)
+        errs = field_errors(em, torch, ch, out["vertices"], out["field"], ln,
+                            samples, seed + 1)
+        blk[prec] = {"gpair_s": out["gpairs"], "ms": out["perf"].time * 1e3,
+                     "pairs": out["perf"].pairs,
+                     "mean_len": float(ln.double().mean()),
+                     "classes": {"steps": int(cls[0]), "charge": int(cls[1]),
+                                 "null": int(cls[2])},
+                     "fp64_refines": out["perf"].fp64_refines,
+                     "field_err_vs_fp64": errs}
+        del out
+        torch.cuda.empty_cache()
+    if with_ratio:
+        # per-pair cost without termination: every line runs 200 rows
+        r = {}
+        for p in ("fp32", "mixed", "fp64"):
+            out = traced(em, torch, ch, seeds, 200, 0.0, p, False)
+            r[p] = out["gpairs"]
+        blk["no_termination_200_rows_gpair_s"] = r
+        blk["mixed_vs_fp32"] = r["mixed"] / r["fp32"]
+        blk["mixed_vs_fp64"] = r["mixed"] / r["fp64"]
+    return blk
+
+
+def adjoint_block(em, torch, dev, seed):
+    """Adjoint: 1024 charges (cube side 100), 16384 lines x 4000 rows; the
+    loss is sum |v - t|^2 against a seeded perturbed copy of the forward."""
+    ch_np, seeds_np, rows = em.workloads.make("adjoint_1024", seed=seed)
+    n = len(seeds_np)
+    ch = torch.from_numpy(np.ascontiguousarray(ch_np, np.float32)).to(dev)
+    V = torch.zeros((3, rows, n), dtype=torch.float32, device=dev)
+    V[:, 0, :] = torch.from_numpy(seeds_np.T.astype(np.float32)).to(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    rc, _ = em.calc_field(V[0].reshape(-1), V[1].reshape(-1), V[2].reshape(-1),
+                          ch, n, 1.0, True, require_n64=False)
+    if rc:
+        raise em.EmError(rc, "forward")
+    T = V + 0.1 * torch.randn(V.shape, generator=gen, device=dev)
+    W = torch.zeros_like(V)
+    W[:, 0, :] = V[:, 0, :]
+    em.adjoint_device(W, ch, T)  # warm-up
+    loss, grad, fwd_s, bwd_s = em.adjoint_device(W, ch, T)
+    torch.cuda.synchronize()
+    pairs = float(n) * (rows - 1) * len(ch_np)
+    return {"workload": "adjoint_1024", "lines": n, "charges": len(ch_np),
+            "rows": rows, "forward_ms": fwd_s * 1e3, "adjoint_ms": bwd_s * 1e3,
+            "adjoint_over_forward": bwd_s / fwd_s,
+            "forward_gpair_s": pairs / fwd_s / 1e9,
+            "loss": float(loss.item()),
+            "grad_norm": float(grad.norm().item()),
+            "checkpoint_rows": 64}
+
+
+def run_extras(em, torch, dev, args):
+    out = {}
+    out["precision"] = precision_block(em, torch, dev, args.workload, 5000,
+                                       args.seed, 20000, True)
+    out["precision_stress"] = precision_block(em, torch, dev, "dipole_16384",
+                                              4000, args.seed, 20000, False)
+    out["adjoint"] = adjoint_block(em, torch, dev, args.seed)
+    torch.cuda.empty_cache()
+    return out
 
 
 def lib_peak(lib):

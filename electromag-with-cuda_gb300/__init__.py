@@ -5,7 +5,8 @@ Import with importlib (the directory name carries hyphens):
 """
 from . import _capi, tracer, workloads  # noqa: F401
 from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
-from .tracer import (adjoint, calc_field, field, new_lines, seed_fibonacci,  # noqa: F401
+from .tracer import (adjoint, adjoint_device, calc_field, field,  # noqa: F401
+                     new_lines, seed_fibonacci,
                      trace_lines, trace_loss_function)
 
 __all__ = ["calc_field", "field", "new_lines", "trace_lines", "seed_fibonacci", "load", "declared_symbols", "strerror",

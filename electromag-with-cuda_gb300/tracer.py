@@ -311,3 +311,32 @@ def trace_loss_function():
             return gout * g, None, None, None, None, None
 
     return TraceLoss
+
+
+def adjoint_device(V, charges, targets, resolution=1.0, use_curvature=True,
+                   stream=None):
+    """em_adjoint_f32 on CUDA torch tensors: V (3, rows, n) float32 with the
+    seeds in row 0 (rows written by the forward), charges (p, 4), targets
+    (3, rows, n).  Returns (loss, grad (p, 4) float64 tensor, fwd_s, bwd_s)."""
+    import torch
+    lib = _capi.load()
+    rows, n = V.shape[1], V.shape[2]
+    p = charges.shape[0]
+    loss = torch.zeros(1, dtype=torch.float64, device=V.device)
+    grad = torch.zeros((p, 4), dtype=torch.float64, device=V.device)
+    o = _capi.EmOptions()
+    o.device_ptrs = 1
+    o.stream = (stream if stream is not None else
+                torch.cuda.current_stream(V.device).cuda_stream)
+    fwd, bwd = _capi.EmPerf(), _capi.EmPerf()
+    ch = charges.contiguous()
+    T = targets.contiguous()
+    rc = lib.em_adjoint_f32(V[0].data_ptr(), V[1].data_ptr(), V[2].data_ptr(),
+                            n, rows, ch.data_ptr(), p, resolution,
+                            int(bool(use_curvature)), T[0].data_ptr(),
+                            T[1].data_ptr(), T[2].data_ptr(), loss.data_ptr(),
+                            grad.data_ptr(), ctypes_byref(o),
+                            ctypes_byref(fwd), ctypes_byref(bwd))
+    if rc:
+        raise _capi.EmError(rc, "em_adjoint_f32")
+    return loss, grad, fwd.time, bwd.time

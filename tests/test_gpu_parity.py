@@ -233,3 +233,16 @@ def test_field_exact_matches_reference_fp32_bitwise(em, gpu, orc, cpu_config):
     e_ref2 = orc.field_f32(pts, ch, three_arg=False)
     e_gpu2 = em.field(pts, ch, arith="exact", rule="generic")
     assert np.array_equal(e_ref2, e_gpu2)
+
+
+def test_field_f64_matches_fp64_oracle(em, gpu, orc, cpu_config):
+    """The GPU FP64 field (the reference's double sequence) equals the CPU
+    FP64 oracle to rounding; bench.py uses it as the FP64 reference for its
+    error statistics."""
+    ch, seeds, _ = cpu_config
+    rng = np.random.default_rng(9)
+    pts = rng.uniform(-60, 60, (4000, 3))
+    e_cpu = orc.field_f64(pts, ch.astype(np.float64))
+    e_gpu = em.field(pts, ch.astype(np.float64), arith="exact")
+    rel = np.linalg.norm(e_gpu - e_cpu, axis=1) / np.linalg.norm(e_cpu, axis=1)
+    assert rel.max() <= 1e-13, rel.max()
