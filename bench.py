@@ -29,6 +29,9 @@ METRIC = ("Gpair-int/s vs plain FP32 at ≤1e-6 field err vs FP64; "
           "adjoint/fwd time ratio")
 UNIT = "Gpair-int/s"
 FLOP_PER_PAIR = 20  # the FP32-roofline credit per pair interaction
+# DRAM bytes (read + write) per trace launch of the 4096-charge workload at
+# 5000 rows, from the ncu launch list in profiles/ref_trace_kernel_gpu4096.md
+TRAFFIC_GPU4096 = 1.911e9 + 7.8e6
 
 
 def parse():
@@ -51,6 +54,9 @@ def parse():
     ap.add_argument("--pack", default="auto")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the extended / precision / adjoint blocks")
+    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint"],
+                    default=None,
+                    help="profiling cases: run one small case and exit")
     return ap.parse_args()
 
 
@@ -195,10 +201,43 @@ def run_reference(args):
     return 0
 
 
+def run_case(args):
+    """Small profiling cases (ncu captures): the extended kernel on the
+    4096-charge workload (200 rows, no termination radius), or the adjoint
+    kernels on the 1024-charge workload (200 rows)."""
+    import torch
+    em = importlib.import_module("electromag-with-cuda_gb300")
+    dev = torch.device("cuda", 0)
+    if args.case.startswith("ext"):
+        ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)
+        ch = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).to(dev)
+        s = torch.from_numpy(seeds.astype(np.float32)).to(dev)
+        prec = args.case.split("-")[1]
+        for _ in range(2):
+            out = em.trace_lines(s, ch, 200, 1.0, 0.0, precision=prec)
+        torch.cuda.synchronize()
+        print(prec, out["perf"].pairs / out["perf"].time / 1e9, "Gpair/s")
+        return 0
+    ch_np, seeds_np, _ = em.workloads.make("adjoint_1024", seed=args.seed)
+    rows, n = 200, len(seeds_np)
+    ch = torch.from_numpy(np.ascontiguousarray(ch_np, np.float32)).to(dev)
+    V = torch.zeros((3, rows, n), dtype=torch.float32, device=dev)
+    V[:, 0, :] = torch.from_numpy(seeds_np.T.astype(np.float32)).to(dev)
+    T = V.clone()
+    for _ in range(2):
+        W = V.clone()
+        _, _, f, b = em.adjoint_device(W, ch, T)
+    torch.cuda.synchronize()
+    print("fwd ms", f * 1e3, "bwd ms", b * 1e3, "ratio", b / f)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        return run_case(args)
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -295,7 +334,9 @@ def main():
                          % (3 * 4 * n * rows / 1e9)},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops,
                      "unit": "TFLOP/s", "frac": achieved / peak_tflops,
-                     "traffic": None,
+                     "traffic": (TRAFFIC_GPU4096 if args.workload == "gpu_4096"
+                                 and not args.rows else None),
+                     "algorithmic_bytes": 12.0 * n * (rows - 1),
                      "peak_source": "measured FFMA peak (em_fp32_peak_tflops)",
                      "flop_per_pair": FLOP_PER_PAIR,
                      "kernel_ms": kernel_s * 1e3},
