@@ -178,6 +178,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     prm.tile_recs = tile;
     prm.stages = cfg.stages;
     prm.resident = cfg.resident;
+    prm.regroup = o.deterministic ? 0 : 1;
     prm.err = c.err;
 
     e = cudaEventRecord(c.ev0, s);

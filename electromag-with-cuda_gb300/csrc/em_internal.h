@@ -82,6 +82,7 @@ template <class T> struct ExtParams {
     int *len, *cls;
     unsigned long long *next_line, *evals, *refines;
     int p_pad, n_tiles, tile_recs, stages, resident;
+    int regroup;                    // widen lane groups once the queue is dry
     int *err;
 };
 

@@ -307,6 +307,77 @@ __device__ __forceinline__ void step_vector(T ex, T ey, T ez, T r0x, T r0y, T r0
     sz = div_rn(ez, s);
 }
 
+
+// ---- group-size dispatch -------------------------------------------------
+// A warp's lane groups start TPL lanes wide and may double (up to the whole
+// warp) when the work queue runs dry; the pair loops stay specialised per
+// width, chosen once per step-iteration.
+template <class T, int MODE, class Rec>
+__device__ __forceinline__ void tile_pairs(int tg, const Rec *tile, int jn, int count, int t,
+                                           const ExtLane<T> &st, T &ax, T &ay, T &az, T &dneg,
+                                           float &dall, CF &hx, CF &hy, CF &hz)
+{
+#define EM_TILE_PAIRS(G)                                                                       \
+    if constexpr (MODE == EXT_MIXED)                                                           \
+        pairs_mixed<G>(tile, jn, count, t, st.px, st.py, st.pz, hx, hy, hz, dneg, dall);       \
+    else                                                                                       \
+        pairs_fast<G>(tile, jn, count, t, st.px, st.py, st.pz, ax, ay, az, dneg);
+    switch (tg) {
+    case 4: EM_TILE_PAIRS(4) break;
+    case 8: EM_TILE_PAIRS(8) break;
+    case 16: EM_TILE_PAIRS(16) break;
+    default: EM_TILE_PAIRS(32) break;
+    }
+#undef EM_TILE_PAIRS
+}
+
+template <class T, int MODE>
+__device__ __forceinline__ void combine_group(int tg, T &ax, T &ay, T &az, T &dneg, float &dall,
+                                              CF &hx, CF &hy, CF &hz)
+{
+#define EM_COMBINE(G)                                                                          \
+    if constexpr (MODE == EXT_MIXED) {                                                         \
+        group_two_sum<G>(hx);                                                                  \
+        group_two_sum<G>(hy);                                                                  \
+        group_two_sum<G>(hz);                                                                  \
+        ax = (T)__fadd_rn(hx.h, hx.l);                                                         \
+        ay = (T)__fadd_rn(hy.h, hy.l);                                                         \
+        az = (T)__fadd_rn(hz.h, hz.l);                                                         \
+        dall = group_min<float, G>(dall);                                                      \
+    } else {                                                                                   \
+        ax = group_sum<T, G>(ax);                                                              \
+        ay = group_sum<T, G>(ay);                                                              \
+        az = group_sum<T, G>(az);                                                              \
+    }                                                                                          \
+    dneg = group_min<T, G>(dneg);
+    switch (tg) {
+    case 4: { EM_COMBINE(4) } break;
+    case 8: { EM_COMBINE(8) } break;
+    case 16: { EM_COMBINE(16) } break;
+    default: { EM_COMBINE(32) } break;
+    }
+#undef EM_COMBINE
+}
+
+__device__ __forceinline__ void fp64_field_group(int tg, const float4 *charges, int count, int t,
+                                                 double px, double py, double pz, double &fx,
+                                                 double &fy, double &fz, bool redo)
+{
+#define EM_FP64(G)                                                                             \
+    if (redo)                                                                                  \
+        field_fp64<G>(charges, count, t, px, py, pz, fx, fy, fz);                              \
+    fx = group_sum<double, G>(fx);                                                             \
+    fy = group_sum<double, G>(fy);                                                             \
+    fz = group_sum<double, G>(fz);
+    switch (tg) {
+    case 4: { EM_FP64(4) } break;
+    case 8: { EM_FP64(8) } break;
+    case 16: { EM_FP64(16) } break;
+    default: { EM_FP64(32) } break;
+    }
+#undef EM_FP64
+}
+
 template <class T, int TPL, int MODE>
 __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P)
 {
@@ -386,9 +457,10 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
     }
 
     // ---- line slots ------------------------------------------------------------
-    const int t = lane % TPL;
-    const int grp_leader = lane - t;
+    int tg = TPL;                   // current lanes per line
+    int t = lane & (tg - 1);
     const long long total_slots = (long long)gridDim.x * ncw * LG;
+    bool queue_empty = total_slots >= P.n;
     long long line = ((long long)blockIdx.x * ncw + warp) * LG + lane / TPL;
     int s = 1, lim = 0;
     ExtLane<T> st;
@@ -434,9 +506,11 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             if (lane == first)
                 base = atomicAdd(P.next_line, (unsigned long long)__popc(m));
             base = __shfl_sync(0xffffffffu, base, first);
+            if ((long long)(base + __popc(m)) + total_slots >= P.n)
+                queue_empty = true;
             const long long mine =
                 (long long)(base + __popc(m & ((1u << lane) - 1u))) + total_slots;
-            const long long nl = __shfl_sync(0xffffffffu, mine, grp_leader);
+            const long long nl = __shfl_sync(0xffffffffu, mine, lane - t);
             if (need) {
                 if (nl < P.n) {
                     line = nl;
@@ -452,6 +526,40 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
     };
     refill();
 
+    // With no lines left to hand out, a warp whose live lines fit in half
+    // of its groups compacts them into wider groups (more lanes per line),
+    // so the last, longest lines run on more lanes.
+    auto regroup = [&]() {
+        if (!P.regroup || !queue_empty || tg >= 32)
+            return;
+        const unsigned lead = __ballot_sync(0xffffffffu, t == 0 && live);
+        const int nlive = __popc(lead);
+        int ng = tg;
+        while (ng < 32 && nlive <= (32 / ng) / 2)
+            ng *= 2;
+        if (ng == tg)
+            return;
+        const int k = lane / ng;
+        const bool has = k < nlive;
+        const int src = has ? (int)__fns(lead, 0, k + 1) : 0;
+        line = __shfl_sync(0xffffffffu, line, src);
+        s = __shfl_sync(0xffffffffu, s, src);
+        lim = __shfl_sync(0xffffffffu, lim, src);
+        st.px = __shfl_sync(0xffffffffu, st.px, src);
+        st.py = __shfl_sync(0xffffffffu, st.py, src);
+        st.pz = __shfl_sync(0xffffffffu, st.pz, src);
+        st.dx = __shfl_sync(0xffffffffu, st.dx, src);
+        st.dy = __shfl_sync(0xffffffffu, st.dy, src);
+        st.dz = __shfl_sync(0xffffffffu, st.dz, src);
+        live = has;
+        need = false;
+        if (!has)
+            line = -1;
+        tg = ng;
+        t = lane & (tg - 1);
+    };
+    regroup();
+
     uint32_t it = 0;
     bool failed = false;
     for (;;) {
@@ -463,12 +571,8 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         float dall = 3.0e38f;
         CF hx, hy, hz;
         if (!streamed) {
-            if constexpr (MODE == EXT_MIXED)
-                pairs_mixed<TPL>(tiles, jneg_all, P.p_pad, t, st.px, st.py, st.pz, hx, hy, hz,
-                                 dneg, dall);
-            else
-                pairs_fast<TPL>(tiles, jneg_all, P.p_pad, t, st.px, st.py, st.pz, ax, ay, az,
-                                dneg);
+            tile_pairs<T, MODE>(tg, tiles, jneg_all, P.p_pad, t, st, ax, ay, az, dneg, dall, hx,
+                                hy, hz);
         } else {
             for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
                 const uint32_t sg = it % NST, ph = (it / NST) & 1;
@@ -480,12 +584,8 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
                     const int base = tile * P.tile_recs;
                     const int jn = min(max(jneg_all - base, 0), P.tile_recs);
                     const Rec *tp = tiles + sg * P.tile_recs;
-                    if constexpr (MODE == EXT_MIXED)
-                        pairs_mixed<TPL>(tp, jn, P.tile_recs, t, st.px, st.py, st.pz, hx, hy,
-                                         hz, dneg, dall);
-                    else
-                        pairs_fast<TPL>(tp, jn, P.tile_recs, t, st.px, st.py, st.pz, ax, ay,
-                                        az, dneg);
+                    tile_pairs<T, MODE>(tg, tp, jn, P.tile_recs, t, st, ax, ay, az, dneg, dall,
+                                        hx, hy, hz);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(empty0 + 8 * sg);
@@ -499,20 +599,7 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             }
         }
         // ---- combine the group's lanes -------------------------------------
-        if constexpr (MODE == EXT_MIXED) {
-            group_two_sum<TPL>(hx);
-            group_two_sum<TPL>(hy);
-            group_two_sum<TPL>(hz);
-            ax = (T)__fadd_rn(hx.h, hx.l);
-            ay = (T)__fadd_rn(hy.h, hy.l);
-            az = (T)__fadd_rn(hz.h, hz.l);
-            dall = group_min<float, TPL>(dall);
-        } else {
-            ax = group_sum<T, TPL>(ax);
-            ay = group_sum<T, TPL>(ay);
-            az = group_sum<T, TPL>(az);
-        }
-        dneg = group_min<T, TPL>(dneg);
+        combine_group<T, MODE>(tg, ax, ay, az, dneg, dall, hx, hy, hz);
         ax = mul_rn(ax, K);
         ay = mul_rn(ay, K);
         az = mul_rn(az, K);
@@ -526,13 +613,9 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             const bool redo = live && !(e2 >= lim2 * lim2);
             if (__any_sync(0xffffffffu, redo)) {
                 double fx = 0, fy = 0, fz = 0;
-                if (redo)
-                    field_fp64<TPL>(reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
-                                    (double)(float)st.px, (double)(float)st.py,
-                                    (double)(float)st.pz, fx, fy, fz);
-                fx = group_sum<double, TPL>(fx);
-                fy = group_sum<double, TPL>(fy);
-                fz = group_sum<double, TPL>(fz);
+                fp64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
+                                 (double)(float)st.px, (double)(float)st.py,
+                                 (double)(float)st.pz, fx, fy, fz, redo);
                 if (redo) {
                     ax = (T)(fx * kElectroK);
                     ay = (T)(fy * kElectroK);
@@ -597,6 +680,7 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             }
         }
         refill();
+        regroup();
     }
     // counters: one atomic per warp
     for (int o = 16; o; o >>= 1) {

@@ -165,7 +165,8 @@ _PREC = {"fp32": _capi.EM_PREC_FP32, "mixed": _capi.EM_PREC_MIXED}
 def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
                 steps_per_line=None, precision="fp32", want_field=False,
                 threads_per_line=0, warps_per_cta=0, tile_charges=0,
-                force_streamed=False, null_frac=0.0, stream=None):
+                force_streamed=False, null_frac=0.0, deterministic=False,
+                stream=None):
     """Extended method (seeded lines, termination, step limits).
 
     seeds (n, 3), charges (p, 4): numpy arrays (host entry point) or CUDA
@@ -184,6 +185,7 @@ def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
     o.tile_charges = tile_charges
     o.force_streamed = int(bool(force_streamed))
     o.null_frac = null_frac
+    o.deterministic = int(bool(deterministic))
     perf = _capi.EmPerf()
     fn = lib.em_trace_lines_f64 if f64 else lib.em_trace_lines_f32
     if _is_torch(seeds):

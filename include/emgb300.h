@@ -96,6 +96,11 @@ typedef struct em_options {
     double null_frac;     /* mixed: FP64 re-evaluation where |E| is below this
                              fraction of the largest single contribution
                              (0: 1e-4)                                       */
+    int deterministic;    /* extended tracer: 1 keeps every line on its
+                             initial lane group, so results repeat bit for
+                             bit; 0 (default) lets warps widen the groups of
+                             their last lines once no lines are left to hand
+                             out (faster tails, last-bit differences)        */
 } em_options;
 
 /* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
