@@ -7,7 +7,7 @@ from . import _capi, tracer, workloads  # noqa: F401
 from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
 from .tracer import (adjoint, adjoint_device, calc_field, field,  # noqa: F401
                      new_lines, seed_fibonacci,
-                     trace_lines, trace_loss_function)
+                     trace_batch, trace_lines, trace_loss_function)
 
 __all__ = ["calc_field", "field", "new_lines", "trace_lines", "seed_fibonacci", "load", "declared_symbols", "strerror",
            "EmError", "workloads"]

@@ -50,6 +50,13 @@ class EmPerf(ctypes.Structure):
                 ("pairs", D), ("wall_time", D), ("fp64_refines", D)]
 
 
+class EmBatchOptions(ctypes.Structure):
+    _fields_ = [("threads_per_line", I), ("lines_per_item", I),
+                ("first_budget", I), ("phases", I), ("tile_charges", I),
+                ("stages", I), ("use_graph", I), ("deterministic", I),
+                ("device_ptrs", I), ("stream", P)]
+
+
 class EmOptions(ctypes.Structure):
     _fields_ = [("arith", I), ("rule", I), ("require_n64", I),
                 ("device_ptrs", I), ("stream", P), ("threads_per_line", I),
@@ -70,6 +77,8 @@ _SIGNATURES = {
     "em_trace_lines_f64": (I, [P, P, P, S, S, P, P, S, D, D, P, P, P, P, P,
                                P, P]),
     "em_seed_fibonacci_f32": (I, [P, S, S, F, P, P, P, S, P]),
+    "em_trace_batch_f32": (I, [S, P, P, P, P, P, P, P, I, F, F, I, P, P, P,
+                               P, P, P, P, P, P, P]),
     "em_adjoint_f32": (I, [P, P, P, S, S, P, S, F, I, P, P, P, P, P, P, P,
                            P]),
     "em_field_f32": (I, [P, P, P, S, P, S, P, P, P, P]),

@@ -360,6 +360,7 @@ int em_release(void)
                     std::make_pair(&c->lines, &c->lines_cap),
                     std::make_pair(&c->scratch, &c->scratch_cap),
                     std::make_pair(&c->adj, &c->adj_cap),
+                    std::make_pair(&c->batch, &c->batch_cap),
                     std::make_pair(&c->errbuf, &c->errbuf_cap)}) {
         if (*pr.first)
             cudaFree(*pr.first);

@@ -115,6 +115,56 @@ int adjoint_charge_blocks(int p);
 cudaError_t launch_adjoint_backward(const AdjParams &P, int nsm, size_t smem, double *loss,
                                     double *grad, cudaStream_t stream);
 
+// Batched tracing (em_trace_batch.cu).
+struct BatchParams {
+    const float4 *staged;        // every set's staged charges
+    const long long *soff;       // per set: first staged record
+    const int *spad, *snneg;     // per set: staged records, padded negative block
+    const float *sqabs;          // per set: largest |q|
+    const long long *coff;       // per set: first charge record (nsets + 1)
+    const float *sx, *sy, *sz;   // seeds of every line (global line ids)
+    const int *steps_per_line;   // optional per-line limits
+    int max_steps;
+    long long nlines;
+    const int4 *items;           // {set, begin, end, 0}; begin/end: line ids (phase 0)
+                                 // or positions in cont_in (later phases)
+    const int *nitems;
+    unsigned *item_ctr;
+    const long long *cont_in;    // later phases: line ids sorted by set
+    float *st_x, *st_y, *st_z;   // saved state of deferred lines
+    int *st_s;
+    long long *cont_out;         // lines deferred by this phase
+    unsigned long long *cont_count;
+    int budget;                  // field evaluations per line in this phase (0: no limit)
+    int phase;
+    float *vx, *vy, *vz;         // rows < store_rows of every line: row * nlines + line
+    int store_rows;
+    float *lx, *ly, *lz;         // last vertex
+    int *len, *cls;
+    double res, term_r2;
+    unsigned long long *evals;   // pair interactions evaluated
+    int resident_cap, tile_recs, stages, regroup;
+    int *err;
+};
+struct BatchQueues {
+    const long long *cont;           // lines deferred by the finished phase
+    unsigned long long *cont_count;  // their number (reset by the sort)
+    long long *cont_sorted;          // the same ids grouped by set
+    int *set_count, *set_fill, *set_item_off;
+    long long *set_line_off;
+    int4 *next_items;
+    int *next_nitems;
+    unsigned *next_item_ctr;
+};
+cudaError_t launch_batch_stage(const float *raw, const long long *coff, const long long *soff,
+                               const int *spad, int gran, int nsets, float *staged, int *snneg,
+                               float *sqabs, cudaStream_t stream);
+cudaError_t launch_batch_sort(const BatchQueues &q, const long long *line_off, int nsets,
+                              int item_lines, cudaStream_t stream);
+cudaError_t prepare_batch_trace(size_t smem);
+cudaError_t launch_batch_trace(const BatchParams &p, int tpl, int grid, int threads, size_t smem,
+                               cudaStream_t stream);
+
 struct LaunchCfg {
     int tpl;     // threads per line (1, 2, 4, 8)
     int kl;      // lines per lane (1, 2; 2 only for the fast forms)

@@ -34,6 +34,8 @@ struct DevCtx {
     size_t scratch_cap = 0;
     void *adj = nullptr;     // adjoint workspace
     size_t adj_cap = 0;
+    void *batch = nullptr;   // batched-tracer workspace
+    size_t batch_cap = 0;
     int *err = nullptr;
 };
 

@@ -28,37 +28,12 @@
 //              FP64, and an FP64 re-evaluation of the whole field where
 //              |E| < null_frac * (largest single contribution bound).
 #include "em_device.cuh"
+#include "em_ext.cuh"
 #include "em_internal.h"
 #include "em_math.cuh"
 
 namespace em {
 namespace {
-
-constexpr int kChunk = 64; // pairs per lane between compensated additions
-
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-    s = __fadd_rn(a, b);
-    const float bp = __fsub_rn(s, a);
-    const float ap = __fsub_rn(s, bp);
-    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
-}
-
-// Compensated value (hi, lo).
-struct CF {
-    float h = 0, l = 0;
-    __device__ __forceinline__ void add(float v)
-    {
-        float e;
-        two_sum(h, v, h, e);
-        l = __fadd_rn(l, e);
-    }
-};
-
-template <class T> struct ExtLane {
-    T px, py, pz;         // evaluation point (FP32 copy in mixed mode)
-    double dx, dy, dz;    // mixed: FP64 position accumulator
-};
 
 // ---------------------------------------------------------------------------
 // Staging: stable partition of p raw records into
@@ -124,258 +99,6 @@ __global__ void __launch_bounds__(1024)
         meta[0] = neg_pad;
         *qabs = m;
     }
-}
-
-// ---------------------------------------------------------------------------
-// Pair loops over shared-memory records [0, count) of one tile, lane t of
-// TPL; [0, jneg) are negative charges (nearest one tracked).
-template <int TPL>
-__device__ __forceinline__ void pairs_fast(const float4 *tile, int jneg, int count, int t,
-                                           float px, float py, float pz, float &ax, float &ay,
-                                           float &az, float &dneg)
-{
-#pragma unroll 4
-    for (int j = t; j < jneg; j += TPL) {
-        const float4 c = tile[j];
-        const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        dneg = fminf(dneg, r2);
-        const float inv = rsqrt_fast(r2);
-        const float s = (c.w * inv) * (inv * inv);
-        ax = fmaf(s, dx, ax);
-        ay = fmaf(s, dy, ay);
-        az = fmaf(s, dz, az);
-    }
-#pragma unroll 8
-    for (int j = jneg + t; j < count; j += TPL) {
-        const float4 c = tile[j];
-        const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const float inv = rsqrt_fast(r2);
-        const float s = (c.w * inv) * (inv * inv);
-        ax = fmaf(s, dx, ax);
-        ay = fmaf(s, dy, ay);
-        az = fmaf(s, dz, az);
-    }
-}
-
-template <int TPL>
-__device__ __forceinline__ void pairs_fast(const ChargeD *tile, int jneg, int count, int t,
-                                           double px, double py, double pz, double &ax,
-                                           double &ay, double &az, double &dneg)
-{
-    for (int j = t; j < count; j += TPL) {
-        const double2 *r = reinterpret_cast<const double2 *>(tile + j);
-        const double2 a = r[0], b = r[1];
-        const double dx = px - a.x, dy = py - a.y, dz = pz - b.x;
-        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-        if (j < jneg)
-            dneg = fmin(dneg, r2);
-        const double inv = rsqrt(r2);
-        const double s = (b.y * inv) * (inv * inv);
-        ax = fma(s, dx, ax);
-        ay = fma(s, dy, ay);
-        az = fma(s, dz, az);
-    }
-}
-
-// Mixed: FP32 pairs with the inv^3 correction over records [lo, hi) (lo a
-// multiple of TPL), compensated every kChunk pairs; dmin gets the nearest
-// distance^2 of the range.
-template <int TPL>
-__device__ __forceinline__ void mixed_range(const float4 *tile, int lo, int hi, int t, float px,
-                                            float py, float pz, CF &hx, CF &hy, CF &hz,
-                                            float &dmin)
-{
-    for (int j0 = lo + t; j0 < hi; j0 += TPL * kChunk) {
-        const int j1 = min(hi, j0 + TPL * kChunk);
-        float ax = 0, ay = 0, az = 0;
-#pragma unroll 4
-        for (int j = j0; j < j1; j += TPL) {
-            const float4 c = tile[j];
-            const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            dmin = fminf(dmin, r2);
-            const float inv = rsqrt_fast(r2);
-            const float inv2 = inv * inv;
-            const float s0 = (c.w * inv) * inv2;
-            // inv^3 carries three times the relative error eps of inv; to
-            // first order r2 inv2 - 1 = 2 eps, so s0 (2.5 - 1.5 r2 inv2) =
-            // s0 / (1 + 3 eps): one Newton correction, three FMA-pipe ops
-            const float g = fmaf(-1.5f * r2, inv2, 2.5f);
-            const float sc = s0 * g;
-            ax = fmaf(sc, dx, ax);
-            ay = fmaf(sc, dy, ay);
-            az = fmaf(sc, dz, az);
-        }
-        hx.add(ax);
-        hy.add(ay);
-        hz.add(az);
-    }
-}
-
-template <int TPL>
-__device__ __forceinline__ void pairs_mixed(const float4 *tile, int jneg, int count, int t,
-                                            float px, float py, float pz, CF &hx, CF &hy, CF &hz,
-                                            float &dneg, float &dall)
-{
-    float dn = 3.0e38f, dp = 3.0e38f;
-    mixed_range<TPL>(tile, 0, jneg, t, px, py, pz, hx, hy, hz, dn);
-    mixed_range<TPL>(tile, jneg, count, t, px, py, pz, hx, hy, hz, dp);
-    dneg = fminf(dneg, dn);
-    dall = fminf(dall, fminf(dn, dp));
-}
-
-// FP64 field at (px, py, pz) from the staged records in global memory, lane
-// t of TPL (summed later across the group).
-template <int TPL>
-__device__ __forceinline__ void field_fp64(const float4 *charges, int count, int t, double px,
-                                           double py, double pz, double &ax, double &ay,
-                                           double &az)
-{
-    for (int j = t; j < count; j += TPL) {
-        const float4 c = charges[j];
-        const double dx = px - (double)c.x, dy = py - (double)c.y, dz = pz - (double)c.z;
-        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-        const double inv = 1.0 / sqrt(r2);
-        const double s = (double)c.w * inv * inv * inv;
-        ax = fma(s, dx, ax);
-        ay = fma(s, dy, ay);
-        az = fma(s, dz, az);
-    }
-}
-
-template <class T, int TPL>
-__device__ __forceinline__ T group_min(T v)
-{
-#pragma unroll
-    for (int o = TPL / 2; o >= 1; o >>= 1)
-        v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-template <int TPL>
-__device__ __forceinline__ void group_two_sum(CF &c)
-{
-#pragma unroll
-    for (int o = TPL / 2; o >= 1; o >>= 1) {
-        const float oh = __shfl_xor_sync(0xffffffffu, c.h, o);
-        const float ol = __shfl_xor_sync(0xffffffffu, c.l, o);
-        // both partners compute the same sum: order the operands by lane
-        // half so the bits agree
-        float a = c.h, b = oh, la = c.l, lb = ol;
-        if ((threadIdx.x & o) != 0) {
-            a = oh;
-            b = c.h;
-            la = ol;
-            lb = c.l;
-        }
-        float s, e;
-        two_sum(a, b, s, e);
-        c.h = s;
-        c.l = __fadd_rn(__fadd_rn(la, lb), e);
-    }
-}
-
-template <class T, int TPL>
-__device__ __forceinline__ T group_sum(T v)
-{
-#pragma unroll
-    for (int o = TPL / 2; o >= 1; o >>= 1) {
-        const T w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (threadIdx.x & o) ? w + v : v + w;
-    }
-    return v;
-}
-
-// Step vector of the reference rule (CPU_Implement.cpp:327-331): returns
-// E / ((k+1) res |E|) with the reference's IEEE sequence; k2 = |E|^2.
-template <class T>
-__device__ __forceinline__ void step_vector(T ex, T ey, T ez, T r0x, T r0y, T r0z, T res, T &sx,
-                                            T &sy, T &sz, T &k2)
-{
-    k2 = add_rn(add_rn(mul_rn(ex, ex), mul_rn(ey, ey)), mul_rn(ez, ez));
-    const T ix = sub_rn(ex, r0x), iy = sub_rn(ey, r0y), iz = sub_rn(ez, r0z);
-    const T cx = sub_rn(mul_rn(iy, r0z), mul_rn(iz, r0y));
-    const T cy = sub_rn(mul_rn(iz, r0x), mul_rn(ix, r0z));
-    const T cz = sub_rn(mul_rn(ix, r0y), mul_rn(iy, r0x));
-    const T c2 = add_rn(add_rn(mul_rn(cx, cx), mul_rn(cy, cy)), mul_rn(cz, cz));
-    const T kc = div_rn(sqrt_rn(c2), mul_rn(k2, sqrt_rn(k2)));
-    const T s = mul_rn(mul_rn(add_rn(kc, T(1)), res), sqrt_rn(k2));
-    sx = div_rn(ex, s);
-    sy = div_rn(ey, s);
-    sz = div_rn(ez, s);
-}
-
-
-// ---- group-size dispatch -------------------------------------------------
-// A warp's lane groups start TPL lanes wide and may double (up to the whole
-// warp) when the work queue runs dry; the pair loops stay specialised per
-// width, chosen once per step-iteration.
-template <class T, int MODE, class Rec>
-__device__ __forceinline__ void tile_pairs(int tg, const Rec *tile, int jn, int count, int t,
-                                           const ExtLane<T> &st, T &ax, T &ay, T &az, T &dneg,
-                                           float &dall, CF &hx, CF &hy, CF &hz)
-{
-#define EM_TILE_PAIRS(G)                                                                       \
-    if constexpr (MODE == EXT_MIXED)                                                           \
-        pairs_mixed<G>(tile, jn, count, t, st.px, st.py, st.pz, hx, hy, hz, dneg, dall);       \
-    else                                                                                       \
-        pairs_fast<G>(tile, jn, count, t, st.px, st.py, st.pz, ax, ay, az, dneg);
-    switch (tg) {
-    case 4: EM_TILE_PAIRS(4) break;
-    case 8: EM_TILE_PAIRS(8) break;
-    case 16: EM_TILE_PAIRS(16) break;
-    default: EM_TILE_PAIRS(32) break;
-    }
-#undef EM_TILE_PAIRS
-}
-
-template <class T, int MODE>
-__device__ __forceinline__ void combine_group(int tg, T &ax, T &ay, T &az, T &dneg, float &dall,
-                                              CF &hx, CF &hy, CF &hz)
-{
-#define EM_COMBINE(G)                                                                          \
-    if constexpr (MODE == EXT_MIXED) {                                                         \
-        group_two_sum<G>(hx);                                                                  \
-        group_two_sum<G>(hy);                                                                  \
-        group_two_sum<G>(hz);                                                                  \
-        ax = (T)__fadd_rn(hx.h, hx.l);                                                         \
-        ay = (T)__fadd_rn(hy.h, hy.l);                                                         \
-        az = (T)__fadd_rn(hz.h, hz.l);                                                         \
-        dall = group_min<float, G>(dall);                                                      \
-    } else {                                                                                   \
-        ax = group_sum<T, G>(ax);                                                              \
-        ay = group_sum<T, G>(ay);                                                              \
-        az = group_sum<T, G>(az);                                                              \
-    }                                                                                          \
-    dneg = group_min<T, G>(dneg);
-    switch (tg) {
-    case 4: { EM_COMBINE(4) } break;
-    case 8: { EM_COMBINE(8) } break;
-    case 16: { EM_COMBINE(16) } break;
-    default: { EM_COMBINE(32) } break;
-    }
-#undef EM_COMBINE
-}
-
-__device__ __forceinline__ void fp64_field_group(int tg, const float4 *charges, int count, int t,
-                                                 double px, double py, double pz, double &fx,
-                                                 double &fy, double &fz, bool redo)
-{
-#define EM_FP64(G)                                                                             \
-    if (redo)                                                                                  \
-        field_fp64<G>(charges, count, t, px, py, pz, fx, fy, fz);                              \
-    fx = group_sum<double, G>(fx);                                                             \
-    fy = group_sum<double, G>(fy);                                                             \
-    fz = group_sum<double, G>(fz);
-    switch (tg) {
-    case 4: { EM_FP64(4) } break;
-    case 8: { EM_FP64(8) } break;
-    case 16: { EM_FP64(16) } break;
-    default: { EM_FP64(32) } break;
-    }
-#undef EM_FP64
 }
 
 template <class T, int TPL, int MODE>

@@ -342,3 +342,78 @@ def adjoint_device(V, charges, targets, resolution=1.0, use_curvature=True,
     if rc:
         raise _capi.EmError(rc, "em_adjoint_f32")
     return loss, grad, fwd.time, bwd.time
+
+
+def trace_batch(sets, max_steps, resolution=1.0, term_radius=0.5, *,
+                steps_per_line=None, store_rows=0, threads_per_line=0,
+                lines_per_item=0, first_budget=0, phases=0, tile_charges=0,
+                stages=0, use_graph=False, deterministic=False, stream=None):
+    """Batched extended method (em_trace_batch_f32).
+
+    sets: list of (charges (p, 4), seeds (m, 3)) numpy arrays, or a dict of
+    concatenated CUDA tensors {charges, seeds, charge_off, line_off} (the
+    offsets as host int64 numpy arrays).  steps_per_line: concatenated
+    per-line limits or None.  Returns dict(len, cls, last (N, 3),
+    rows (3, store_rows, N) or None, perf, charge_off, line_off)."""
+    lib = _capi.load()
+    o = _capi.EmBatchOptions()
+    o.threads_per_line = threads_per_line
+    o.lines_per_item = lines_per_item
+    o.first_budget = first_budget
+    o.phases = phases
+    o.tile_charges = tile_charges
+    o.stages = stages
+    o.use_graph = int(bool(use_graph))
+    o.deterministic = int(bool(deterministic))
+    perf = _capi.EmPerf()
+    if isinstance(sets, dict):
+        import torch
+        ch = sets["charges"].contiguous()
+        sd = sets["seeds"].contiguous()
+        coff = np.ascontiguousarray(sets["charge_off"], np.int64)
+        loff = np.ascontiguousarray(sets["line_off"], np.int64)
+        N = int(loff[-1])
+        dev = ch.device
+        S = sd.T.contiguous()
+        last = torch.empty((3, N), dtype=torch.float32, device=dev)
+        ln = torch.empty(N, dtype=torch.int32, device=dev)
+        cl = torch.empty(N, dtype=torch.int32, device=dev)
+        R = (torch.empty((3, store_rows, N), dtype=torch.float32, device=dev)
+             if store_rows else None)
+        spl = (steps_per_line.to(torch.int32).contiguous()
+               if steps_per_line is not None else None)
+        o.device_ptrs = 1
+        o.stream = (stream if stream is not None else
+                    torch.cuda.current_stream(dev).cuda_stream)
+        ptr = lambda a: a.data_ptr()  # noqa: E731
+    else:
+        coff = np.zeros(len(sets) + 1, np.int64)
+        loff = np.zeros(len(sets) + 1, np.int64)
+        for i, (c, s) in enumerate(sets):
+            coff[i + 1] = coff[i] + len(c)
+            loff[i + 1] = loff[i] + len(s)
+        ch = np.ascontiguousarray(np.concatenate([np.asarray(c, np.float32)
+                                                  for c, _ in sets]))
+        sd = np.concatenate([np.asarray(s, np.float32) for _, s in sets])
+        S = np.ascontiguousarray(sd.T)
+        N = int(loff[-1])
+        last = np.zeros((3, N), np.float32)
+        ln = np.zeros(N, np.int32)
+        cl = np.zeros(N, np.int32)
+        R = np.zeros((3, store_rows, N), np.float32) if store_rows else None
+        spl = (np.ascontiguousarray(steps_per_line, np.int32)
+               if steps_per_line is not None else None)
+        ptr = lambda a: a.ctypes.data  # noqa: E731
+    rc = lib.em_trace_batch_f32(
+        len(coff) - 1, ptr(ch), coff.ctypes.data, ptr(S[0]), ptr(S[1]),
+        ptr(S[2]), loff.ctypes.data, ptr(spl) if spl is not None else None,
+        max_steps, resolution, term_radius, store_rows,
+        ptr(R[0]) if R is not None else None,
+        ptr(R[1]) if R is not None else None,
+        ptr(R[2]) if R is not None else None,
+        ptr(last[0]), ptr(last[1]), ptr(last[2]), ptr(ln), ptr(cl),
+        ctypes_byref(o), ctypes_byref(perf))
+    if rc:
+        raise _capi.EmError(rc, "em_trace_batch_f32")
+    return dict(len=ln, cls=cl, last=last.T, rows=R, perf=perf,
+                charge_off=coff, line_off=loff)

@@ -210,6 +210,43 @@ EM_API int em_adjoint_f32(float *x, float *y, float *z, size_t n, size_t rows,
                           const float *tz, double *loss, double *grad,
                           const em_options *opt, em_perf *fwd, em_perf *bwd);
 
+/* Batched tracing of many independent charge sets (the extended method) in
+ * persistent launches fed by a device work queue (no counterpart in the
+ * reference, which traces one set per call).  Set s owns charge records
+ * [charge_off[s], charge_off[s+1]) and lines [line_off[s], line_off[s+1])
+ * (global line ids; charge_off and line_off are HOST arrays of nsets+1).
+ * Seeds sx/sy/sz, optional steps_per_line and the outputs are indexed by
+ * global line id: len, cls, the last vertex lx/ly/lz, and the first
+ * store_rows rows of every line in vx/vy/vz (row * nlines + line; may be
+ * NULL when store_rows == 0).  Host pointers unless opt->device_ptrs.
+ * perf->pairs counts field evaluations x the set's charge count. */
+typedef struct em_batch_options {
+    int threads_per_line; /* 0: 8; else 4, 8 or 16 (lanes per line)         */
+    int lines_per_item;   /* 0: 512 lines per work item                      */
+    int first_budget;     /* 0: 256 field evaluations per line in phase 0;
+                             each later phase has four times more, the last
+                             is unlimited                                    */
+    int phases;           /* 0: 4                                            */
+    int tile_charges;     /* 0: 1024; tile of sets too large for shared
+                             memory                                          */
+    int stages;           /* 0: 4; ring depth for those sets                 */
+    int use_graph;        /* 1: capture the launches into a CUDA graph and
+                             replay it                                       */
+    int deterministic;    /* 1: no lane-group widening (bit-repeatable)      */
+    int device_ptrs;
+    void *stream;
+} em_batch_options;
+EM_API int em_trace_batch_f32(size_t nsets, const float *charges,
+                              const int64_t *charge_off, const float *sx,
+                              const float *sy, const float *sz,
+                              const int64_t *line_off,
+                              const int32_t *steps_per_line, int max_steps,
+                              float resolution, float term_radius,
+                              int store_rows, float *vx, float *vy, float *vz,
+                              float *lx, float *ly, float *lz, int32_t *len,
+                              int32_t *cls, const em_batch_options *opt,
+                              em_perf *perf);
+
 /* Seeds on a sphere of `radius` around every positive charge (q > 0), in
  * charge order: lines_per_charge golden-angle spiral directions
  * (z_i = 1 - (2i+1)/L, phi_i = i * pi (3 - sqrt 5)).  Writes at most cap
