@@ -458,8 +458,65 @@ def adjoint_block(em, torch, dev, seed):
             "checkpoint_rows": 64}
 
 
+def batch_block(em, torch, dev, seed):
+    """512 independent sets (sizes log-uniform in [64, 32768], cube side 100,
+    4 lines per positive charge, step limits per set uniform in [500, 8000],
+    termination at negative charges): one graph-captured batched launch
+    sequence with autotuned shape, against per-set launches of the single-set
+    tracer (same FP32 arithmetic)."""
+    sets = em.workloads.make_batch(512, seed)
+    max_steps = max(lim for _, _, lim in sets)
+    lims = np.concatenate([np.full(len(s), lim, np.int32) for _, s, lim in sets])
+    pairs_sets = [(c, s) for c, s, _ in sets]
+    t0 = time.perf_counter()
+    opts = em.autotune.tune_batch(pairs_sets, max_steps, lims, sample=16,
+                                  use_cache=False)
+    tune_s = time.perf_counter() - t0
+    coff = np.concatenate([[0], np.cumsum([len(c) for c, _, _ in sets])])
+    loff = np.concatenate([[0], np.cumsum([len(s) for _, s, _ in sets])])
+    d = {"charges": torch.from_numpy(np.concatenate([c for c, _, _ in sets])
+                                     .astype(np.float32)).to(dev),
+         "seeds": torch.from_numpy(np.concatenate([s for _, s, _ in sets])).to(dev),
+         "charge_off": coff, "line_off": loff}
+    spl = torch.from_numpy(lims).to(dev)
+    em.trace_batch(d, max_steps, 1.0, 0.5, steps_per_line=spl, use_graph=True,
+                   **opts)
+    torch.cuda.synchronize()
+    r = em.trace_batch(d, max_steps, 1.0, 0.5, steps_per_line=spl,
+                       use_graph=True, **opts)
+    torch.cuda.synchronize()
+    bt, bp = r["perf"].time, r["perf"].pairs
+    cls = np.bincount(r["cls"].cpu().numpy(), minlength=3)
+    # per-set launches of the single-set tracer
+    ksum, psum = 0.0, 0.0
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for (c, s, lim) in sets:
+        out = em.trace_lines(torch.from_numpy(s).to(dev),
+                             torch.from_numpy(np.ascontiguousarray(c, np.float32))
+                             .to(dev), lim, 1.0, 0.5)
+        ksum += out["perf"].time
+        psum += out["perf"].pairs
+        del out
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    torch.cuda.empty_cache()
+    return {"workload": "batch_512", "sets": len(sets), "lines": int(loff[-1]),
+            "charges": int(coff[-1]), "max_rows": max_steps,
+            "tuned": opts, "tune_seconds": tune_s,
+            "batched_ms": bt * 1e3, "batched_pairs": bp,
+            "batched_gpair_s": bp / bt / 1e9,
+            "classes": {"steps": int(cls[0]), "charge": int(cls[1]),
+                        "null": int(cls[2])},
+            "per_set_kernel_ms": ksum * 1e3, "per_set_wall_ms": wall * 1e3,
+            "per_set_pairs": psum, "per_set_gpair_s": psum / ksum / 1e9,
+            "speedup_vs_per_set_kernels": ksum / bt,
+            "speedup_vs_per_set_wall": wall / bt}
+
+
 def run_extras(em, torch, dev, args):
     out = {}
+    out["batched"] = batch_block(em, torch, dev, args.seed)
     out["precision"] = precision_block(em, torch, dev, args.workload, 5000,
                                        args.seed, 20000, True)
     out["precision_stress"] = precision_block(em, torch, dev, "dipole_16384",

@@ -3,7 +3,7 @@
 Import with importlib (the directory name carries hyphens):
     em = importlib.import_module("electromag-with-cuda_gb300")
 """
-from . import _capi, tracer, workloads  # noqa: F401
+from . import _capi, autotune, shard, tracer, workloads  # noqa: F401
 from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
 from .tracer import (adjoint, adjoint_device, calc_field, field,  # noqa: F401
                      new_lines, seed_fibonacci,

@@ -5,7 +5,9 @@
 // The _f32/_f64 entry points take host pointers and return when the result
 // is in the caller's arrays, like CalcField_CPU<T> (CPU_Implement.cpp:501).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <cstdlib>
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -49,10 +51,24 @@ DevCtx *get_ctx(int *code)
     return &c;
 }
 
+// Host-side fault injection for tests: EM_INJECT_ALLOC_FAIL=<k> makes the
+// k-th device allocation of the process fail (counting from 1).
+static bool inject_alloc_failure()
+{
+    static long long target = [] {
+        const char *v = std::getenv("EM_INJECT_ALLOC_FAIL");
+        return v ? std::atoll(v) : 0LL;
+    }();
+    static std::atomic<long long> count{0};
+    return target > 0 && ++count == target;
+}
+
 int grow(void **buf, size_t *cap, size_t need)
 {
     if (need <= *cap && *buf)
         return EM_OK;
+    if (inject_alloc_failure())
+        return EM_ERR_NOMEM;
     if (*buf) {
         cudaFree(*buf);
         *buf = nullptr;

@@ -66,8 +66,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 }
 
 // Waits for the phase with the given parity to complete.  Returns false
-// (and records a timeout in *err) if it has not completed within the limit.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err)
+// (and records a timeout in *err) if it has not completed within limit_ns.
+__device__ __forceinline__ bool mbar_wait_limit(uint32_t bar, uint32_t parity, int *err,
+                                                uint64_t limit_ns)
 {
     if (mbar_try_wait(bar, parity))
         return true;
@@ -76,13 +77,18 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *er
         for (int i = 0; i < 64; ++i)
             if (mbar_try_wait(bar, parity))
                 return true;
-        if (globaltimer_ns() - t0 > EM_WAIT_LIMIT_NS) {
+        if (globaltimer_ns() - t0 > limit_ns) {
             atomicCAS(err, 0, EM_DEVERR_TIMEOUT);
             return false;
         }
         if (*(volatile int *)err != 0)
             return false; // another warp already gave up
     }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err)
+{
+    return mbar_wait_limit(bar, parity, err, EM_WAIT_LIMIT_NS);
 }
 
 // Bulk copy of `bytes` (multiple of 16, both addresses 16-B aligned) from

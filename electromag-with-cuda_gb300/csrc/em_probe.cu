@@ -3,6 +3,7 @@
 // library has launched in the process.
 #include <atomic>
 
+#include "em_device.cuh"
 #include "em_internal.h"
 #include "emgb300.h"
 
@@ -37,10 +38,58 @@ __global__ void __launch_bounds__(512) ffma_peak_kernel(float *out, int iters, f
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// One warp waits on an mbarrier that nothing completes, with a short limit:
+// the bounded-wait path every tracer kernel relies on, exercised on purpose.
+__global__ void wait_selftest_kernel(int *err, unsigned long long limit_ns)
+{
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        mbar_init(b, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    mbar_wait_limit(b, 0, err, limit_ns);
+}
+
 } // namespace
 } // namespace em
 
 extern "C" {
+
+int em_selftest_wait_timeout(int limit_ms, double *elapsed_ms)
+{
+    if (limit_ms < 1 || limit_ms > 5000)
+        return EM_ERR_ARG;
+    int *err = nullptr;
+    if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_NOMEM;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemset(err, 0, sizeof(int));
+    cudaEventRecord(e0);
+    em::wait_selftest_kernel<<<1, 32>>>(err, (unsigned long long)limit_ms * 1000000ull);
+    cudaEventRecord(e1);
+    em::count_launch(1);
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, err, sizeof(int), cudaMemcpyDeviceToHost);
+    float ms = 0;
+    if (e == cudaSuccess)
+        cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(err);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_CUDA;
+    }
+    if (elapsed_ms)
+        *elapsed_ms = ms;
+    return v == em::EM_DEVERR_TIMEOUT ? EM_ERR_TIMEOUT : (v ? EM_ERR_CUDA : EM_OK);
+}
 
 int em_fp32_peak_tflops(double *tflops, double *seconds)
 {

@@ -1,0 +1,37 @@
+"""Sharding of independent field lines across ranks (one GPU per rank).
+
+Lines never interact, so the path shards by contiguous line ranges with no
+exchange during tracing; results are gathered only if the caller wants them
+in one place.  The reference's multi-device split
+(GPGPU_Segment/src/CL_Electrostatics.cpp:113-183) sizes shares by compute
+units; here ranks are identical GPUs, so shares differ by at most one line.
+"""
+import numpy as np
+
+
+def shard_range(n, world, rank):
+    """Contiguous [begin, end) of n lines for `rank` of `world`."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad world/rank")
+    base, extra = divmod(n, world)
+    begin = rank * base + min(rank, extra)
+    return begin, begin + base + (1 if rank < extra else 0)
+
+
+def gather_lines(local, n, world, rank, group=None):
+    """All ranks receive the full (n, ...) array from each rank's shard
+    (torch.distributed all_gather over padded shards)."""
+    import torch
+    import torch.distributed as dist
+    b, e = shard_range(n, world, rank)
+    width = (n + world - 1) // world
+    t = torch.as_tensor(np.asarray(local))
+    pad = torch.zeros((width,) + tuple(t.shape[1:]), dtype=t.dtype)
+    pad[: e - b] = t
+    parts = [torch.zeros_like(pad) for _ in range(world)]
+    dist.all_gather(parts, pad, group=group)
+    out = []
+    for r in range(world):
+        rb, re_ = shard_range(n, world, r)
+        out.append(parts[r][: re_ - rb])
+    return torch.cat(out).numpy()

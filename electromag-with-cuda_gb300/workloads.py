@@ -85,3 +85,20 @@ def make(name, seed=1234, dtype=np.float32):
     else:
         seeds = fibonacci_seeds(ch, cfg["lines_per_positive"])
     return ch, seeds, cfg["steps"]
+
+
+def make_batch(nsets=512, seed=1234, pmin=64, pmax=32768, half=50.0,
+               lines_per_positive=4, steps=(500, 8000)):
+    """Independent charge sets for batched tracing: sizes log-uniform in
+    [pmin, pmax], charges uniform in [-half, half]^3 with |q| in U[1, 10] and
+    random sign, lines_per_positive seeds per positive charge, one step limit
+    per set uniform in `steps`.  Returns a list of (charges, seeds, limit)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.exp(rng.uniform(np.log(pmin), np.log(pmax), nsets)).astype(int)
+    limits = rng.integers(steps[0], steps[1] + 1, nsets)
+    out = []
+    for i, (p, lim) in enumerate(zip(sizes, limits)):
+        ch = uniform_charges(int(p), half, seed * 7919 + i)
+        seeds = fibonacci_seeds(ch, lines_per_positive).astype(np.float32)
+        out.append((ch, seeds, int(lim)))
+    return out

@@ -283,6 +283,12 @@ EM_API const char *em_strerror(int code);
  * tracer's FP32 roofline.  em_launch_count: kernels this library has
  * launched in this process. */
 EM_API int em_fp32_peak_tflops(double *tflops, double *seconds);
+/* Failure-path self-test: one warp waits on a device barrier that nothing
+ * completes, bounded by limit_ms (1..5000).  Every device-side wait of the
+ * tracer kernels is bounded the same way.  Returns EM_ERR_TIMEOUT when the
+ * wait expired and the kernel returned as designed (the device stays
+ * usable); *elapsed_ms gets the kernel's duration. */
+EM_API int em_selftest_wait_timeout(int limit_ms, double *elapsed_ms);
 EM_API unsigned long long em_launch_count(void);
 /* Library version, "major.minor.patch". */
 EM_API const char *em_version(void);

@@ -1,0 +1,64 @@
+"""Line sharding across ranks: two gloo ranks on CPU each trace their shard
+of lines with the CPU oracle and gather; the result equals one process
+tracing every line (lines are independent: no exchange while tracing)."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+
+def test_shard_ranges_cover_exactly(em):
+    for n in (0, 1, 7, 64, 1000):
+        for w in (1, 2, 3, 8):
+            got = []
+            for r in range(w):
+                b, e = em.shard.shard_range(n, w, r)
+                got.extend(range(b, e))
+            assert got == list(range(n))
+            sizes = [em.shard.shard_range(n, w, r) for r in range(w)]
+            assert max(e - b for b, e in sizes) - min(e - b for b, e in sizes) <= 1
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, world, port, out_path):
+    import importlib
+    import sys
+    import torch.distributed as dist
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    sys.path.insert(0, os.path.join(root, "oracle"))
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    em = importlib.import_module("electromag-with-cuda_gb300")
+    import em_oracle as orc
+    ch, seeds, _ = em.workloads.make("cpu_256", seed=4)
+    n, steps = len(seeds), 30
+    b, e = em.shard.shard_range(n, world, rank)
+    _, ln, cl = orc.trace_lines_f64(ch.astype(np.float64), seeds[b:e], steps,
+                                    1.0, 0.5, nthreads=1)
+    L = em.shard.gather_lines(ln, n, world, rank)
+    C = em.shard.gather_lines(cl, n, world, rank)
+    if rank == 0:
+        np.savez(out_path, len=L, cls=C)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_equal_single_process(em, orc, tmp_path):
+    out = str(tmp_path / "gathered.npz")
+    mp.spawn(_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    g = np.load(out)
+    ch, seeds, _ = em.workloads.make("cpu_256", seed=4)
+    _, ln, cl = orc.trace_lines_f64(ch.astype(np.float64), seeds, 30, 1.0, 0.5)
+    assert np.array_equal(g["len"], ln)
+    assert np.array_equal(g["cls"], cl)
