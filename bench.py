@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--pack", default="auto")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the extended / precision / adjoint blocks")
-    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint"],
+    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint",
+                                       "adjoint-checkpoint"],
                     default=None,
                     help="profiling cases: run one small case and exit")
     return ap.parse_args()
@@ -204,7 +205,8 @@ def run_reference(args):
 def run_case(args):
     """Small profiling cases (ncu captures): the extended kernel on the
     4096-charge workload (200 rows, no termination radius), or the adjoint
-    kernels on the 1024-charge workload (200 rows)."""
+    kernels on the 1024-charge workload (200 rows; stored field, or the
+    field recomputed per 64-row segment)."""
     import torch
     em = importlib.import_module("electromag-with-cuda_gb300")
     dev = torch.device("cuda", 0)
@@ -226,7 +228,8 @@ def run_case(args):
     T = V.clone()
     for _ in range(2):
         W = V.clone()
-        _, _, f, b = em.adjoint_device(W, ch, T)
+        _, _, f, b = em.adjoint_device(
+            W, ch, T, checkpoint=args.case == "adjoint-checkpoint")
     torch.cuda.synchronize()
     print("fwd ms", f * 1e3, "bwd ms", b * 1e3, "ratio", b / f)
     return 0
@@ -445,17 +448,22 @@ def adjoint_block(em, torch, dev, seed):
     T = V + 0.1 * torch.randn(V.shape, generator=gen, device=dev)
     W = torch.zeros_like(V)
     W[:, 0, :] = V[:, 0, :]
-    em.adjoint_device(W, ch, T)  # warm-up
-    loss, grad, fwd_s, bwd_s = em.adjoint_device(W, ch, T)
-    torch.cuda.synchronize()
     pairs = float(n) * (rows - 1) * len(ch_np)
-    return {"workload": "adjoint_1024", "lines": n, "charges": len(ch_np),
-            "rows": rows, "forward_ms": fwd_s * 1e3, "adjoint_ms": bwd_s * 1e3,
-            "adjoint_over_forward": bwd_s / fwd_s,
-            "forward_gpair_s": pairs / fwd_s / 1e9,
-            "loss": float(loss.item()),
-            "grad_norm": float(grad.norm().item()),
-            "checkpoint_rows": 64}
+    blk = {"workload": "adjoint_1024", "lines": n, "charges": len(ch_np),
+           "rows": rows}
+    # stored: the forward keeps its field at every vertex; checkpoint: only
+    # the vertices, the field recomputed per 64-row segment
+    for mode, ck in (("stored", False), ("checkpoint", True)):
+        em.adjoint_device(W, ch, T, checkpoint=ck)  # warm-up
+        loss, grad, fwd_s, bwd_s = em.adjoint_device(W, ch, T, checkpoint=ck)
+        torch.cuda.synchronize()
+        blk[mode] = {"forward_ms": fwd_s * 1e3, "adjoint_ms": bwd_s * 1e3,
+                     "adjoint_over_forward": bwd_s / fwd_s,
+                     "forward_gpair_s": pairs / fwd_s / 1e9,
+                     "loss": float(loss.item()),
+                     "grad_norm": float(grad.norm().item())}
+    blk["checkpoint_rows"] = 64
+    return blk
 
 
 def batch_block(em, torch, dev, seed):

@@ -63,7 +63,8 @@ class EmOptions(ctypes.Structure):
                 ("warps_per_cta", I), ("tile_charges", I),
                 ("force_streamed", I), ("pack", I),
                 ("lines_per_thread", I), ("precision", I),
-                ("null_frac", D), ("deterministic", I)]
+                ("null_frac", D), ("deterministic", I),
+                ("adjoint_checkpoint", I)]
 
 
 _SIGNATURES = {

@@ -10,14 +10,29 @@
 //   dL/dc_j = -q_j sum_s G(r_sj) mu_s,   dL/dq_j = sum_s r_sj . mu_s / |r_sj|^3
 //   G(r) mu = mu/|r|^3 - 3 r (r . mu)/|r|^5            (K cancels throughout)
 //
-// Schedule: the forward writes every vertex (the caller's output).  The
-// backward walks segments of P.seg rows (64: the line-state checkpoint
-// interval) from the end.  Per segment,
+// The backward needs E'_s at every vertex.  Either the forward stores it
+// (12 B per vertex), or only the vertices are kept (the line state at every
+// row, which the forward writes anyway) and the field is recomputed per
+// segment of 64 rows, walking the segments from the end; the recompute
+// repeats the forward's lane order, so it gives the same bits and the same
+// lam_s.
+//
+// Fused backward (p <= kAdjFusedMaxCharges).  The pair term G(r_sj) mu_s
+// feeds both sums: over charges for the line's a_s, over rows and lines for
+// charge j's gradient.  A team of W warps takes one line at a time and walks
+// its rows backwards; lane l of warp w owns charges k*32W + 32w + l (k < CPL)
+// and keeps their four gradient sums in registers across all the rows and
+// lines it processes, flushing them every 512 rows into compensated (hi, lo)
+// partials of its team.  Each pair is formed once (26 FP32 ops + one rsqrt)
+// instead of twice.  Per block of 32 rows, lane l prepares row (top - l):
+// u, lam/|E'|, the vertex and 2 (v - t); each row then takes them from that
+// lane by shuffle.
+//
+// Two-pass backward (larger p, up to the shared-memory limit): per segment,
 // adj_line_kernel (TPL lanes per line, charges resident in shared memory)
-// recomputes E at each stored vertex (the same lane order as the forward, so
-// the same bits and the same lam), forms mu, runs the Jacobian-vector pair
-// loop and writes (v_s, mu_s) records; adj_charge_kernel then keeps a few
-// charges per thread in registers and streams the segment's records
+// recomputes E at each stored vertex, forms mu, runs the Jacobian-vector
+// pair loop and writes (v_s, mu_s) records; adj_charge_kernel then keeps a
+// few charges per thread in registers and streams the segment's records
 // (L2-resident) to accumulate the charge gradients into FP64 partial sums,
 // one per (slice of records, charge), summed at the end.
 #include "em_device.cuh"
@@ -253,6 +268,300 @@ __global__ void __launch_bounds__(kChargeThreads) adj_charge_kernel(const AdjPar
     }
 }
 
+// E' = E/K at the stored vertices of rows [s_lo, s_hi), written at row
+// (s - f_row0): the forward's pair loop, lane order and reduction (TPL = 8,
+// charges t, t+8, ...), so the bits equal the forward's.
+__global__ void __launch_bounds__(1024, 1) adj_field_kernel(const AdjParams P, int s_lo, int s_hi)
+{
+    constexpr int TPL = kAdjTpl, LG = 32 / TPL;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    float4 *tiles = reinterpret_cast<float4 *>(smem + 128);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, t = lane % TPL;
+    const uint32_t b0 = smem_addr(bar);
+    if (threadIdx.x == 0) {
+        mbar_init(b0, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)P.p_pad * 16u;
+        mbar_arrive_expect_tx(b0, bytes);
+        const char *src = static_cast<const char *>(P.charges);
+        constexpr uint32_t CH = 32768;
+        for (uint32_t off = 0; off < bytes; off += CH)
+            bulk_g2s(smem_addr(tiles) + off, src + off, bytes - off < CH ? bytes - off : CH, b0);
+    }
+    if (!mbar_wait(b0, 0, P.err))
+        return;
+    const size_t n = (size_t)P.n;
+    const long long groups = (P.n + LG - 1) / LG;
+    const int nw = blockDim.x >> 5;
+    for (long long g = blockIdx.x + (long long)gridDim.x * warp; g < groups;
+         g += (long long)gridDim.x * nw) {
+        const long long line = g * LG + lane / TPL;
+        const bool own = line < P.n;
+        const long long l = own ? line : 0;
+        for (int s = s_lo; s < s_hi; ++s) {
+            const size_t i = (size_t)s * n + l;
+            const float vx = P.x[i], vy = P.y[i], vz = P.z[i];
+            float ex = 0, ey = 0, ez = 0;
+#pragma unroll 8
+            for (int j = t; j < P.p_pad; j += TPL) {
+                const float4 c = tiles[j];
+                const float dx = vx - c.x, dy = vy - c.y, dz = vz - c.z;
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float inv = rsqrt_fast(r2);
+                const float sc = (c.w * inv) * (inv * inv);
+                ex = fmaf(sc, dx, ex);
+                ey = fmaf(sc, dy, ey);
+                ez = fmaf(sc, dz, ez);
+            }
+            ex = lane_sum<TPL>(ex);
+            ey = lane_sum<TPL>(ey);
+            ez = lane_sum<TPL>(ez);
+            if (own && t == 0) {
+                const size_t fi = (size_t)(s - P.f_row0) * n + (size_t)line;
+                P.fx[fi] = ex;
+                P.fy[fi] = ey;
+                P.fz[fi] = ez;
+            }
+        }
+    }
+}
+
+// warp index within its team of W warps
+__device__ __forceinline__ int wt_of(unsigned tid, int W) { return (int)(tid >> 5) % W; }
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float ap = __fsub_rn(s, bp);
+    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+// Adds a lane's register sums into its team's compensated partials and
+// clears them; lane l of warp wt owns records (k*W + wt)*32 + l.
+template <int CPL, int W>
+__device__ __forceinline__ void adj_flush(const AdjParams &P, long long team, int wt, int lane,
+                                          float (&g)[4][CPL])
+{
+    constexpr int PB = 32 * W * CPL;
+    float2 *tp = P.tpart + (size_t)team * 4 * PB + wt * 32 + lane;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+            float2 *q = tp + c * PB + k * W * 32;
+            float2 v = *q;
+            float sum, err;
+            two_sum_f(v.x, g[c][k], sum, err);
+            v.x = sum;
+            v.y = __fadd_rn(v.y, err);
+            *q = v;
+            g[c][k] = 0.0f;
+        }
+    }
+}
+
+// Fused backward over rows [s_lo, s_hi) of every line (see the file
+// comment).  blockDim = 128 (4 warps); teams of W warps.  CPL and W are
+// compile-time so every shared-memory and partial-sum offset is an
+// immediate.
+template <int CPL, int W>
+__global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const AdjParams P,
+                                                                          int s_lo, int s_hi)
+{
+    constexpr int kFlushRows = 512;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    float4 *red = reinterpret_cast<float4 *>(smem + 128); // [2 parities][4 warps]
+    const float4 *ch = reinterpret_cast<const float4 *>(smem + 256) + wt_of(threadIdx.x, W) * 32 +
+                       (threadIdx.x & 31);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tpc = (int)(blockDim.x >> 5) / W;
+    const int team = warp / W, wt = warp - team * W;
+    const uint32_t b0 = smem_addr(bar);
+    if (threadIdx.x == 0) {
+        mbar_init(b0, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)P.p_bwd * 16u;
+        mbar_arrive_expect_tx(b0, bytes);
+        const char *src = static_cast<const char *>(P.charges);
+        constexpr uint32_t CHUNK = 32768;
+        const uint32_t dst = smem_addr(smem + 256);
+        for (uint32_t off = 0; off < bytes; off += CHUNK)
+            bulk_g2s(dst + off, src + off, bytes - off < CHUNK ? bytes - off : CHUNK, b0);
+    }
+    // every warp leaves together if the copy did not land (a team's warps
+    // meet at named barriers later, which must never miss a member)
+    const bool staged = mbar_wait(b0, 0, P.err);
+    if (__syncthreads_or(!staged) || team >= tpc)
+        return;
+    const long long tid = (long long)blockIdx.x * tpc + team;
+    const long long nteams = (long long)gridDim.x * tpc;
+    const size_t n = (size_t)P.n;
+    const float K = (float)kElectroK;
+    const unsigned FULL = 0xffffffffu;
+
+    float g[4][CPL]; // x, y, z gradient sums and -3 sum r.mu/r^3 per owned charge
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int k = 0; k < CPL; ++k)
+            g[c][k] = 0.0f;
+    int acc_rows = 0;
+
+    for (long long line = tid; line < P.n; line += nteams) {
+        float ax = P.abar[line], ay = P.abar[n + line], az = P.abar[2 * n + line];
+        const float p0x = P.x[line], p0y = P.y[line], p0z = P.z[line];
+        for (int bh = s_hi; bh > s_lo; bh -= 32) {
+            const int bl = max(s_lo, bh - 32);
+            // lane l prepares row bh - 1 - l
+            float pux = 0, puy = 0, puz = 0, pf = 0;
+            float pvx = 0, pvy = 0, pvz = 0, pgx = 0, pgy = 0, pgz = 0;
+            const int sl = bh - 1 - lane;
+            if (sl >= bl) {
+                const size_t i = (size_t)sl * n + (size_t)line;
+                pvx = P.x[i];
+                pvy = P.y[i];
+                pvz = P.z[i];
+                pgx = 2.0f * (pvx - P.tx[i]);
+                pgy = 2.0f * (pvy - P.ty[i]);
+                pgz = 2.0f * (pvz - P.tz[i]);
+                const size_t fi = (size_t)(sl - P.f_row0) * n + (size_t)line;
+                const float ex = P.fx[fi], ey = P.fy[fi], ez = P.fz[fi];
+                // lam_s from E = K E' (the forward's IEEE step sequence)
+                const float Ex = mul_rn(ex, K), Ey = mul_rn(ey, K), Ez = mul_rn(ez, K);
+                const float k2 =
+                    add_rn(add_rn(mul_rn(Ex, Ex), mul_rn(Ey, Ey)), mul_rn(Ez, Ez));
+                float lam = 1.0f / P.resolution;
+                if (P.curvature) {
+                    const float ix = sub_rn(Ex, p0x), iy = sub_rn(Ey, p0y), iz = sub_rn(Ez, p0z);
+                    const float cx = sub_rn(mul_rn(iy, p0z), mul_rn(iz, p0y));
+                    const float cy = sub_rn(mul_rn(iz, p0x), mul_rn(ix, p0z));
+                    const float cz = sub_rn(mul_rn(ix, p0y), mul_rn(iy, p0x));
+                    const float c2 =
+                        add_rn(add_rn(mul_rn(cx, cx), mul_rn(cy, cy)), mul_rn(cz, cz));
+                    const float kc = div_rn(sqrt_rn(c2), mul_rn(k2, sqrt_rn(k2)));
+                    lam = 1.0f / mul_rn(add_rn(kc, 1.0f), P.resolution);
+                }
+                const float en = sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
+                const float ien = 1.0f / en;
+                pux = ex * ien;
+                puy = ey * ien;
+                puz = ez * ien;
+                pf = lam * ien;
+            }
+            for (int s = bh - 1; s >= bl; --s) {
+                const int src = bh - 1 - s;
+                const float ux = __shfl_sync(FULL, pux, src), uy = __shfl_sync(FULL, puy, src),
+                            uz = __shfl_sync(FULL, puz, src), f = __shfl_sync(FULL, pf, src);
+                const float vx = __shfl_sync(FULL, pvx, src), vy = __shfl_sync(FULL, pvy, src),
+                            vz = __shfl_sync(FULL, pvz, src);
+                const float gxs = __shfl_sync(FULL, pgx, src), gys = __shfl_sync(FULL, pgy, src),
+                            gzs = __shfl_sync(FULL, pgz, src);
+                // mu' = lam (a - u (u.a)) / |E'|
+                const float ua = fmaf(uz, az, fmaf(uy, ay, ux * ax));
+                const float mx = f * fmaf(-ux, ua, ax), my = f * fmaf(-uy, ua, ay),
+                            mz = f * fmaf(-uz, ua, az);
+                const float m3x = -3.0f * mx, m3y = -3.0f * my, m3z = -3.0f * mz;
+                // G(r) mu = inv3 mu + w3 r, w3 = -3 (r.mu) / r^5
+                float s1 = 0, wx = 0, wy = 0, wz = 0;
+#pragma unroll
+                for (int k = 0; k < CPL; ++k) {
+                    const float4 c = ch[k * W * 32];
+                    const float dx = vx - c.x, dy = vy - c.y, dz = vz - c.z;
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    const float inv = rsqrt_fast(r2);
+                    const float inv2 = inv * inv;
+                    const float inv3 = inv2 * inv;
+                    const float d3 = fmaf(dz, m3z, fmaf(dy, m3y, dx * m3x));
+                    const float hd = d3 * inv3;
+                    const float w3 = hd * inv2;
+                    g[3][k] += hd;
+                    g[0][k] = fmaf(w3, dx, fmaf(inv3, mx, g[0][k]));
+                    g[1][k] = fmaf(w3, dy, fmaf(inv3, my, g[1][k]));
+                    g[2][k] = fmaf(w3, dz, fmaf(inv3, mz, g[2][k]));
+                    s1 = fmaf(c.w, inv3, s1);
+                    const float qw = c.w * w3;
+                    wx = fmaf(qw, dx, wx);
+                    wy = fmaf(qw, dy, wy);
+                    wz = fmaf(qw, dz, wz);
+                }
+#pragma unroll
+                for (int o = 16; o >= 1; o >>= 1) {
+                    s1 += __shfl_xor_sync(FULL, s1, o);
+                    wx += __shfl_xor_sync(FULL, wx, o);
+                    wy += __shfl_xor_sync(FULL, wy, o);
+                    wz += __shfl_xor_sync(FULL, wz, o);
+                }
+                if (W > 1) {
+                    // team sum in warp order, identical in every warp; slots
+                    // alternate by row parity so one barrier per row suffices
+                    float4 *slot = red + (s & 1) * 4;
+                    if (lane == 0)
+                        slot[warp] = make_float4(s1, wx, wy, wz);
+                    asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(32 * W) : "memory");
+                    s1 = wx = wy = wz = 0;
+                    for (int w = 0; w < W; ++w) {
+                        const float4 v = slot[team * W + w];
+                        s1 += v.x;
+                        wx += v.y;
+                        wy += v.z;
+                        wz += v.w;
+                    }
+                }
+                ax = (gxs + ax) + fmaf(s1, mx, wx);
+                ay = (gys + ay) + fmaf(s1, my, wy);
+                az = (gzs + az) + fmaf(s1, mz, wz);
+            }
+            acc_rows += bh - bl;
+            if (acc_rows >= kFlushRows) {
+                adj_flush<CPL, W>(P, tid, wt, lane, g);
+                acc_rows = 0;
+            }
+        }
+        if (wt == 0 && lane == 0) {
+            P.abar[line] = ax;
+            P.abar[n + line] = ay;
+            P.abar[2 * n + line] = az;
+        }
+    }
+    if (acc_rows > 0)
+        adj_flush<CPL, W>(P, tid, wt, lane, g);
+}
+
+// Sums the fused kernel's team partials over one slice of teams into FP64
+// (gpart[slice], the layout adj_finish_kernel reads); the fourth sum holds
+// -3 sum r.mu/r^3 and is scaled back here.
+__global__ void __launch_bounds__(256) adj_team_sum_kernel(const AdjParams P)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= P.p)
+        return;
+    const long long per = (P.teams + gridDim.y - 1) / gridDim.y;
+    const long long t0 = blockIdx.y * per, t1 = min(P.teams, t0 + per);
+    double acc[4] = {0, 0, 0, 0};
+    for (long long t = t0; t < t1; ++t) {
+        const float2 *tp = P.tpart + (size_t)t * 4 * (size_t)P.p_bwd + j;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float2 v = tp[(size_t)c * P.p_bwd];
+            acc[c] += (double)v.x + (double)v.y;
+        }
+    }
+    double *out = P.gpart + ((size_t)blockIdx.y * P.p + j) * 4;
+    out[0] = acc[0];
+    out[1] = acc[1];
+    out[2] = acc[2];
+    out[3] = acc[3] * (-1.0 / 3.0);
+}
+
 // a_{S-1} = 2 (v_{S-1} - t_{S-1}); records also for the last row (mu = 0
 // is never used: the last row has no outgoing step).
 __global__ void adj_init_kernel(const AdjParams P)
@@ -290,11 +599,88 @@ int adjoint_charge_blocks(int p)
     return (p + kChargeThreads * kChargesPerThread - 1) / (kChargeThreads * kChargesPerThread);
 }
 
-cudaError_t launch_adjoint_backward(const AdjParams &P, int nsm, size_t smem, double *loss,
-                                    double *grad, cudaStream_t stream)
+namespace {
+
+void *fused_kernel(int cpl, int w)
+{
+    switch (cpl) {
+    case 4: return (void *)adj_fused_kernel<4, 1>;
+    case 8: return (void *)adj_fused_kernel<8, 1>;
+    case 16: return (void *)adj_fused_kernel<16, 1>;
+    default:
+        return w == 4 ? (void *)adj_fused_kernel<32, 4>
+                      : w == 2 ? (void *)adj_fused_kernel<32, 2> : (void *)adj_fused_kernel<32, 1>;
+    }
+}
+
+} // namespace
+
+int adjoint_fused_plan(int p, int nsm, AdjFused *f)
+{
+    if (p < 1 || p > kAdjFusedMaxCharges)
+        return 0;
+    int cpl = 32, w = 1;
+    if (p <= 128)
+        cpl = 4;
+    else if (p <= 256)
+        cpl = 8;
+    else if (p <= 512)
+        cpl = 16;
+    else
+        w = (p + 1023) / 1024; // 1, 2 or 4 warps per line
+    if (w == 3)
+        w = 4;
+    f->cpl = cpl;
+    f->team_warps = w;
+    f->p_bwd = 32 * w * cpl;
+    f->smem = 256 + (size_t)f->p_bwd * 16;
+    void *k = fused_kernel(cpl, w);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, f->smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    f->grid = nsm * per_sm;
+    f->teams = (long long)f->grid * (4 / w);
+    return 1;
+}
+
+namespace {
+
+cudaError_t launch_fused(const AdjParams &P, const AdjFused &f, int lo, int hi,
+                         cudaStream_t stream)
+{
+    const dim3 grid((unsigned)f.grid);
+    switch (f.cpl * 8 + f.team_warps) {
+    case 4 * 8 + 1: adj_fused_kernel<4, 1><<<grid, 128, f.smem, stream>>>(P, lo, hi); break;
+    case 8 * 8 + 1: adj_fused_kernel<8, 1><<<grid, 128, f.smem, stream>>>(P, lo, hi); break;
+    case 16 * 8 + 1: adj_fused_kernel<16, 1><<<grid, 128, f.smem, stream>>>(P, lo, hi); break;
+    case 32 * 8 + 1: adj_fused_kernel<32, 1><<<grid, 128, f.smem, stream>>>(P, lo, hi); break;
+    case 32 * 8 + 2: adj_fused_kernel<32, 2><<<grid, 128, f.smem, stream>>>(P, lo, hi); break;
+    case 32 * 8 + 4: adj_fused_kernel<32, 4><<<grid, 128, f.smem, stream>>>(P, lo, hi); break;
+    default: return cudaErrorInvalidValue;
+    }
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, int nsm,
+                                    size_t smem, double *loss, double *grad,
+                                    cudaStream_t stream)
 {
     cudaError_t e = cudaFuncSetAttribute(adj_line_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(adj_field_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
     if (e != cudaSuccess)
         return e;
     const size_t elems = (size_t)P.n * (size_t)P.rows;
@@ -302,14 +688,34 @@ cudaError_t launch_adjoint_backward(const AdjParams &P, int nsm, size_t smem, do
     adj_init_kernel<<<(unsigned)((P.n + 255) / 256), 256, 0, stream>>>(P);
     count_launch(2);
     const int seg = P.seg;
-    const dim3 cgrid((unsigned)adjoint_charge_blocks(P.p), (unsigned)P.slices);
-    for (int hi = P.rows - 1; hi > 0; hi -= seg) {
-        const int lo = std::max(0, hi - seg);
-        adj_line_kernel<<<nsm, 1024, smem, stream>>>(P, lo, hi);
-        adj_charge_kernel<<<cgrid, kChargeThreads, 0, stream>>>(P, (long long)(hi - lo) * P.n);
-        count_launch(2);
-        if ((e = cudaGetLastError()) != cudaSuccess)
-            return e;
+    if (fused) {
+        if (P.stored) {
+            if ((e = launch_fused(P, *fused, 0, P.rows - 1, stream)) != cudaSuccess)
+                return e;
+        } else {
+            for (int hi = P.rows - 1; hi > 0; hi -= seg) {
+                const int lo = std::max(0, hi - seg);
+                AdjParams Q = P;
+                Q.f_row0 = lo;
+                adj_field_kernel<<<nsm, 1024, smem, stream>>>(Q, lo, hi);
+                count_launch(1);
+                if ((e = launch_fused(Q, *fused, lo, hi, stream)) != cudaSuccess)
+                    return e;
+            }
+        }
+        const dim3 sgrid((unsigned)((P.p + 255) / 256), (unsigned)P.slices);
+        adj_team_sum_kernel<<<sgrid, 256, 0, stream>>>(P);
+        count_launch(1);
+    } else {
+        const dim3 cgrid((unsigned)adjoint_charge_blocks(P.p), (unsigned)P.slices);
+        for (int hi = P.rows - 1; hi > 0; hi -= seg) {
+            const int lo = std::max(0, hi - seg);
+            adj_line_kernel<<<nsm, 1024, smem, stream>>>(P, lo, hi);
+            adj_charge_kernel<<<cgrid, kChargeThreads, 0, stream>>>(P, (long long)(hi - lo) * P.n);
+            count_launch(2);
+            if ((e = cudaGetLastError()) != cudaSuccess)
+                return e;
+        }
     }
     adj_finish_kernel<<<(P.p + 127) / 128, 128, 0, stream>>>(P, grad);
     count_launch(1);

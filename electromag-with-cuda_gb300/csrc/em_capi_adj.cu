@@ -43,8 +43,12 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     DevCtx &c = *cp;
     std::lock_guard<std::mutex> guard(c.mu);
 
-    // forward shape: 8 lanes per line, one line per lane, scalar pairs: the
-    // order the backward's field recompute repeats bit for bit
+    AdjFused af{};
+    const bool fused = adjoint_fused_plan((int)p, c.nsm, &af) != 0;
+    const bool stored = fused && !o.adjoint_checkpoint;
+    // forward shape: 8 lanes per line, one line per lane, scalar pairs, in
+    // both modes (the order the field recompute repeats bit for bit, so the
+    // two modes trace the same vertices)
     em_options fo{};
     fo.threads_per_line = 8;
     fo.lines_per_thread = 1;
@@ -52,27 +56,40 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     Plan pl;
     if ((code = make_plan<float>(c, n, p, fo, &pl)))
         return code;
-    if (!pl.cfg.resident)
+    if (!pl.cfg.resident && !stored)
         return EM_ERR_TOO_LARGE;
     const size_t elems = n * rows;
     cudaStream_t s = (o.device_ptrs && o.stream) ? (cudaStream_t)o.stream : c.stream;
+    const int p_stage = fused ? std::max(pl.p_pad, af.p_bwd) : pl.p_pad;
 
-    if ((code = grow(&c.charges, &c.charges_cap, (size_t)pl.p_pad * 16)))
+    if ((code = grow(&c.charges, &c.charges_cap, (size_t)p_stage * 16)))
         return code;
     if ((code = grow(&c.charges_raw, &c.charges_raw_cap, p * 16 + 16)))
         return code;
     if ((code = grow(&c.errbuf, &c.errbuf_cap, 256)))
         return code;
     c.err = static_cast<int *>(c.errbuf);
-    const int cb = adjoint_charge_blocks((int)p);
     const long long recs = (long long)kSeg * (long long)n;
-    const int slices = (int)std::max<long long>(
-        1, std::min<long long>(std::max(1, 4 * c.nsm / cb), (recs + 2047) / 2048));
-    // adjoint workspace: abar (3n f32), records (6 * seg * n f32), partials
-    // (slices * p * 4 f64), loss + grad (1 + 4p f64)
-    const size_t off_rec = (3 * n * 4 + 255) / 256 * 256;
-    const size_t off_part = off_rec + (6 * (size_t)recs * 4 + 255) / 256 * 256;
-    const size_t off_loss = off_part + ((size_t)slices * p * 4 * 8 + 255) / 256 * 256;
+    int slices;
+    if (fused) {
+        slices = (int)std::min<long long>(64, af.teams);
+    } else {
+        const int cb = adjoint_charge_blocks((int)p);
+        slices = (int)std::max<long long>(
+            1, std::min<long long>(std::max(1, 4 * c.nsm / cb), (recs + 2047) / 2048));
+    }
+    // adjoint workspace: abar (3n f32); records (6 * seg * n f32, two-pass)
+    // or the field (3 * rows * n f32 stored, 3 * seg * n f32 recomputed) and
+    // the team partials (teams * 4 * p_bwd float2, fused); slice partials
+    // (slices * p * 4 f64); loss + grad (1 + 4p f64)
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t field_rows = stored ? rows : (size_t)kSeg;
+    const size_t off_rec = up(3 * n * 4);
+    const size_t rec_bytes = fused ? 3 * field_rows * n * 4 : 6 * (size_t)recs * 4;
+    const size_t off_tpart = off_rec + up(rec_bytes);
+    const size_t tpart_bytes = fused ? (size_t)af.teams * 4 * (size_t)af.p_bwd * 8 : 0;
+    const size_t off_part = off_tpart + up(tpart_bytes);
+    const size_t off_loss = off_part + up((size_t)slices * p * 4 * 8);
     const size_t off_grad = off_loss + 256;
     const size_t need = off_grad + 4 * p * 8;
     if ((code = grow(&c.adj, &c.adj_cap, need)))
@@ -99,7 +116,7 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(c.charges_raw, charges, p * 16, kin, s);
     if (e == cudaSuccess)
-        e = launch_stage_charges<float>(c.charges_raw, (int)p, c.charges, pl.p_pad, 0,
+        e = launch_stage_charges<float>(c.charges_raw, (int)p, c.charges, p_stage, 0,
                                         pl.cfg.tile_recs, s);
     if (e == cudaSuccess && !o.device_ptrs) {
         const float *src[6] = {x, y, z, tx, ty, tz};
@@ -110,7 +127,7 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
                                 cudaMemcpyHostToDevice, s);
     }
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(ws + off_part, 0, off_grad - off_part, s);
+        e = cudaMemsetAsync(ws + off_tpart, 0, off_grad - off_tpart, s);
     if (e != cudaSuccess)
         return map_cuda(e);
 
@@ -130,6 +147,13 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     prm.rule = use_curvature ? RULE_SSE : RULE_FIXED;
     prm.resolution = resolution;
     prm.err = c.err;
+    float *fbuf = reinterpret_cast<float *>(ws + off_rec);
+    const size_t fstride = field_rows * n;
+    if (stored) {
+        prm.fx = fbuf;
+        prm.fy = fbuf + fstride;
+        prm.fz = fbuf + 2 * fstride;
+    }
 
     AdjParams ap{};
     ap.x = dx;
@@ -153,6 +177,17 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     ap.gpart = reinterpret_cast<double *>(ws + off_part);
     ap.slices = slices;
     ap.err = c.err;
+    if (fused) {
+        ap.fx = fbuf;
+        ap.fy = fbuf + fstride;
+        ap.fz = fbuf + 2 * fstride;
+        ap.f_row0 = 0;
+        ap.stored = stored ? 1 : 0;
+        ap.tpart = reinterpret_cast<float2 *>(ws + off_tpart);
+        ap.p_bwd = af.p_bwd;
+        ap.team_warps = af.team_warps;
+        ap.teams = af.teams;
+    }
     double *dloss = reinterpret_cast<double *>(ws + off_loss);
     double *dgrad = reinterpret_cast<double *>(ws + off_grad);
 
@@ -165,7 +200,8 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     if (e == cudaSuccess)
         e = cudaEventRecord(c.ev1, s);
     if (e == cudaSuccess)
-        e = launch_adjoint_backward(ap, c.nsm, 128 + (size_t)pl.p_pad * 16, dloss, dgrad, s);
+        e = launch_adjoint_backward(ap, fused ? &af : nullptr, c.nsm,
+                                    128 + (size_t)pl.p_pad * 16, dloss, dgrad, s);
     if (e == cudaSuccess)
         e = cudaEventRecord(ev2, s);
     if (e == cudaSuccess)
@@ -207,7 +243,9 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     }
     if (bwd) {
         bwd->time = ms_b * 1e-3;
-        bwd->pairs = 3 * pairs; // field recompute, Jacobian-vector and charge passes
+        // pair passes: fused (1), plus the field recompute (2), or the
+        // recompute, Jacobian-vector and charge passes (3)
+        bwd->pairs = (stored ? 1 : fused ? 2 : 3) * pairs;
         bwd->performance = 0;
         bwd->wall_time = wall;
         bwd->progress = 1.0;

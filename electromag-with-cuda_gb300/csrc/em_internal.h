@@ -55,6 +55,9 @@ template <class T> struct RefTraceParams {
     int rule;                  // Rule
     T resolution;
     int *err;                  // device error word
+    // optional: the charge sum E/K (fast arithmetic) at vertex s of each
+    // line, stored at (s * n + line) for s < total_steps - 1 (null: none)
+    T *fx, *fy, *fz;
 };
 
 // Extended tracer (em_trace_ext.cu).
@@ -110,10 +113,35 @@ struct AdjParams {
     double *gpart;             // slices * p * 4 partial sums
     int slices;
     int *err;
+    // field E/K at the vertices of rows [f_row0, ...) (row stride n): the
+    // forward's own output (f_row0 = 0), or one segment recomputed from the
+    // stored vertices (f_row0 = the segment's first row)
+    float *fx, *fy, *fz;
+    int f_row0;
+    int stored;                // 1: the forward stored the field of every row
+    // fused backward: per team, 4 blocks of p_bwd compensated (hi, lo) sums
+    float2 *tpart;
+    int p_bwd, team_warps;
+    long long teams;
+};
+// Shape of the fused backward (p up to kAdjFusedMaxCharges charges).
+constexpr int kAdjFusedMaxCharges = 4096;
+struct AdjFused {
+    int cpl;          // charges per lane
+    int team_warps;   // warps per line team
+    int p_bwd;        // staged records the fused kernel reads (32 * team_warps * cpl)
+    int grid;         // persistent CTAs
+    long long teams;  // grid * teams per CTA
+    size_t smem;
 };
 int adjoint_charge_blocks(int p);
-cudaError_t launch_adjoint_backward(const AdjParams &P, int nsm, size_t smem, double *loss,
-                                    double *grad, cudaStream_t stream);
+// Fills *f and returns 1 when the fused backward applies to p charges.
+int adjoint_fused_plan(int p, int nsm, AdjFused *f);
+// fused == nullptr: the two-pass backward (field recompute + Jacobian-vector
+// kernel, then the charge-stationary kernel) per 64-row segment.
+cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, int nsm,
+                                    size_t smem, double *loss, double *grad,
+                                    cudaStream_t stream);
 
 // Batched tracing (em_trace_batch.cu).
 struct BatchParams {

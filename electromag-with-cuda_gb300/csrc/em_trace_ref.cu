@@ -282,6 +282,12 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                     ay = line_reduce<T, TPL>(ay);
                     az = line_reduce<T, TPL>(az);
                 }
+                if (P.fx && own[k] && t == 0) {
+                    const size_t fi = (size_t)(step - 1) * n + (size_t)line[k];
+                    store_stream(P.fx + fi, ax);
+                    store_stream(P.fy + fi, ay);
+                    store_stream(P.fz + fi, az);
+                }
                 if (ARITH != ARITH_EXACT) {
                     ax = mul_rn(ax, K);
                     ay = mul_rn(ay, K);

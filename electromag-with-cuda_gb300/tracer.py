@@ -258,13 +258,16 @@ def seed_fibonacci(charges, lines_per_charge, radius=1.0):
     return out[:, : cnt.value].T.copy()
 
 
-def adjoint(seeds, charges, rows, targets, resolution=1.0, use_curvature=True):
+def adjoint(seeds, charges, rows, targets, resolution=1.0, use_curvature=True,
+            checkpoint=False):
     """Loss sum |v - t|^2 over the traced vertices and its gradient with
     respect to the charges (em_adjoint_f32, frozen step lengths).
 
     seeds (n, 3), charges (p, 4), targets (3, rows, n): numpy arrays.
+    checkpoint: keep only the vertices and recompute the field per 64-row
+    segment instead of storing the forward's field.
     Returns dict(loss, grad (p, 4) float64 [dx, dy, dz, dq], vertices
-    (3, rows, n), fwd_time, bwd_time)."""
+    (3, rows, n), fwd_time, bwd_time, bwd_pairs)."""
     lib = _capi.load()
     seeds = np.asarray(seeds, np.float32)
     n = seeds.shape[0]
@@ -276,17 +279,19 @@ def adjoint(seeds, charges, rows, targets, resolution=1.0, use_curvature=True):
     loss = np.zeros(1, np.float64)
     grad = np.zeros((p, 4), np.float64)
     fwd, bwd = _capi.EmPerf(), _capi.EmPerf()
+    o = _capi.EmOptions()
+    o.adjoint_checkpoint = int(bool(checkpoint))
     rc = lib.em_adjoint_f32(V[0].ctypes.data, V[1].ctypes.data,
                             V[2].ctypes.data, n, rows, ch.ctypes.data, p,
                             resolution, int(bool(use_curvature)),
                             T[0].ctypes.data, T[1].ctypes.data,
                             T[2].ctypes.data, loss.ctypes.data,
-                            grad.ctypes.data, None, ctypes_byref(fwd),
-                            ctypes_byref(bwd))
+                            grad.ctypes.data, ctypes_byref(o),
+                            ctypes_byref(fwd), ctypes_byref(bwd))
     if rc:
         raise _capi.EmError(rc, "em_adjoint_f32")
     return dict(loss=float(loss[0]), grad=grad, vertices=V,
-                fwd_time=fwd.time, bwd_time=bwd.time)
+                fwd_time=fwd.time, bwd_time=bwd.time, bwd_pairs=bwd.pairs)
 
 
 def trace_loss_function():
@@ -316,10 +321,11 @@ def trace_loss_function():
 
 
 def adjoint_device(V, charges, targets, resolution=1.0, use_curvature=True,
-                   stream=None):
+                   stream=None, checkpoint=False):
     """em_adjoint_f32 on CUDA torch tensors: V (3, rows, n) float32 with the
     seeds in row 0 (rows written by the forward), charges (p, 4), targets
-    (3, rows, n).  Returns (loss, grad (p, 4) float64 tensor, fwd_s, bwd_s)."""
+    (3, rows, n); checkpoint as in adjoint().  Returns (loss, grad (p, 4)
+    float64 tensor, fwd_s, bwd_s)."""
     import torch
     lib = _capi.load()
     rows, n = V.shape[1], V.shape[2]
@@ -328,6 +334,7 @@ def adjoint_device(V, charges, targets, resolution=1.0, use_curvature=True,
     grad = torch.zeros((p, 4), dtype=torch.float64, device=V.device)
     o = _capi.EmOptions()
     o.device_ptrs = 1
+    o.adjoint_checkpoint = int(bool(checkpoint))
     o.stream = (stream if stream is not None else
                 torch.cuda.current_stream(V.device).cuda_stream)
     fwd, bwd = _capi.EmPerf(), _capi.EmPerf()

@@ -101,6 +101,10 @@ typedef struct em_options {
                              bit; 0 (default) lets warps widen the groups of
                              their last lines once no lines are left to hand
                              out (faster tails, last-bit differences)        */
+    int adjoint_checkpoint; /* em_adjoint_f32: 0 (default) keeps the forward's
+                             field at every vertex (12 more bytes per vertex);
+                             1 keeps only the vertices and recomputes the
+                             field per 64-row segment                        */
 } em_options;
 
 /* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
@@ -199,11 +203,16 @@ EM_API int em_trace_lines_f64(double *x, double *y, double *z, size_t n,
  * lam_s = 1/((k_s+1) res) held at their forward values:
  *   *loss = sum over lines and rows of |v - t|^2 (targets tx, ty, tz),
  *   grad[4j+c] = dL/d(charge j component c), c = x, y, z, q (FP64).
- * The backward recomputes the fields from the stored vertices in segments
- * of 64 rows.  Charges must fit in shared memory (p <= 14000, else
- * EM_ERR_TOO_LARGE).  fwd / bwd (optional) receive the forward and the
- * backward device times (time) and pair counts.  Host pointers unless
- * opt->device_ptrs. */
+ * The backward walks each line from its last row to its first.  For
+ * p <= 4096 one fused pass forms every (vertex, charge) term once and feeds
+ * both the line's adjoint and the charge's gradient; it reads the field the
+ * forward stored at every vertex, or, with opt->adjoint_checkpoint, the field
+ * recomputed from the stored vertices per 64-row segment.  Larger sets run
+ * two passes per 64-row segment (the field recompute with the line adjoint,
+ * then the charge gradients).  Charges must fit in shared memory
+ * (p <= 14000, else EM_ERR_TOO_LARGE).  fwd / bwd (optional) receive the
+ * forward and the backward device times (time) and pair evaluations.  Host
+ * pointers unless opt->device_ptrs. */
 EM_API int em_adjoint_f32(float *x, float *y, float *z, size_t n, size_t rows,
                           const float *charges, size_t p, float resolution,
                           int use_curvature, const float *tx, const float *ty,

@@ -463,20 +463,20 @@ double orc_frozen_loss_cs_f64(const double *charges, size_t p, const double *sx,
     return cimag(L) / h;
 }
 
-double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
-                           const double *sy, const double *sz, size_t n,
-                           size_t S, double res, const double *tx,
-                           const double *ty, const double *tz,
-                           const double *lam_in, double *grad)
+/* Backward sweep of the frozen map along the trajectory vx, vy, vz (S rows
+ * of n lines): the discrete adjoint of CPU_Implement.cpp:322-338's step with
+ * lam_s from lam_in, or, when lam_in is NULL, from the curvature of the
+ * field at the given vertex against the line's row-0 vertex (curvature 0:
+ * lam_s = 1/res).  Adds dL/d(charges) into grad. */
+static void adjoint_sweep(const double *charges, size_t p, const double *vx,
+                          const double *vy, const double *vz, size_t n, size_t S,
+                          double res, int curvature, const double *tx,
+                          const double *ty, const double *tz, const double *lam_in,
+                          double *grad)
 {
-    double *vx = malloc(sizeof(double) * S * n), *vy = malloc(sizeof(double) * S * n),
-           *vz = malloc(sizeof(double) * S * n);
-    const double L = orc_frozen_loss_f64(charges, p, sx, sy, sz, n, S, res, tx, ty,
-                                         tz, lam_in, NULL, vx, vy, vz);
-    for (size_t k = 0; k < 4 * p; ++k)
-        grad[k] = 0;
     for (size_t l = 0; l < n; ++l) {
         const size_t last = (S - 1) * n + l;
+        const double p0[3] = {vx[l], vy[l], vz[l]};
         double a[3] = {2 * (vx[last] - tx[last]), 2 * (vy[last] - ty[last]),
                        2 * (vz[last] - tz[last])};
         for (size_t s = S - 1; s-- > 0;) {
@@ -484,12 +484,14 @@ double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
             const double v[3] = {vx[i], vy[i], vz[i]};
             double e[3];
             field_prime(charges, p, v[0], v[1], v[2], e);
+            const double lam = lam_in ? lam_in[i]
+                               : curvature ? frozen_lambda(e, p0, res) : 1.0 / res;
             const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
             const double u[3] = {e[0] / en, e[1] / en, e[2] / en};
             const double ua = u[0] * a[0] + u[1] * a[1] + u[2] * a[2];
             double mu[3];
             for (int c = 0; c < 3; ++c)
-                mu[c] = lam_in[i] * (a[c] - u[c] * ua) / en;
+                mu[c] = lam * (a[c] - u[c] * ua) / en;
             double jm[3] = {0, 0, 0};
             for (size_t j = 0; j < p; ++j) {
                 const double r[3] = {v[0] - charges[4 * j], v[1] - charges[4 * j + 1],
@@ -509,8 +511,39 @@ double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
                 a[c] = 2 * (v[c] - (c == 0 ? tx[i] : c == 1 ? ty[i] : tz[i])) + a[c] + jm[c];
         }
     }
+}
+
+double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
+                           const double *sy, const double *sz, size_t n,
+                           size_t S, double res, const double *tx,
+                           const double *ty, const double *tz,
+                           const double *lam_in, double *grad)
+{
+    double *vx = malloc(sizeof(double) * S * n), *vy = malloc(sizeof(double) * S * n),
+           *vz = malloc(sizeof(double) * S * n);
+    const double L = orc_frozen_loss_f64(charges, p, sx, sy, sz, n, S, res, tx, ty,
+                                         tz, lam_in, NULL, vx, vy, vz);
+    for (size_t k = 0; k < 4 * p; ++k)
+        grad[k] = 0;
+    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, 1, tx, ty, tz, lam_in, grad);
     free(vx);
     free(vy);
     free(vz);
+    return L;
+}
+
+double orc_adjoint_at_f64(const double *charges, size_t p, const double *vx,
+                          const double *vy, const double *vz, size_t n, size_t S,
+                          double res, int curvature, const double *tx,
+                          const double *ty, const double *tz, double *grad)
+{
+    double L = 0;
+    for (size_t i = 0; i < S * n; ++i) {
+        const double dx = vx[i] - tx[i], dy = vy[i] - ty[i], dz = vz[i] - tz[i];
+        L += dx * dx + dy * dy + dz * dz;
+    }
+    for (size_t k = 0; k < 4 * p; ++k)
+        grad[k] = 0;
+    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, curvature, tx, ty, tz, NULL, grad);
     return L;
 }

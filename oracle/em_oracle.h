@@ -137,6 +137,14 @@ double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
                            size_t S, double res, const double *tx,
                            const double *ty, const double *tz,
                            const double *lam_in, double *grad);
+/* The same discrete adjoint linearised at a given trajectory (vx, vy, vz:
+ * S rows of n lines, e.g. a GPU forward's vertices in FP64), with lam_s
+ * computed from the FP64 field at each given vertex (curvature against the
+ * row-0 vertex; curvature 0: 1/res).  Returns L at that trajectory. */
+double orc_adjoint_at_f64(const double *charges, size_t p, const double *vx,
+                          const double *vy, const double *vz, size_t n, size_t S,
+                          double res, int curvature, const double *tx,
+                          const double *ty, const double *tz, double *grad);
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,9 @@ def load():
         lib.orc_frozen_grad_f64.restype = D
         lib.orc_frozen_grad_f64.argtypes = [P, S, P, P, P, S, S, D, P, P, P,
                                             P, P]
+        lib.orc_adjoint_at_f64.restype = D
+        lib.orc_adjoint_at_f64.argtypes = [P, S, P, P, P, S, S, D, I, P, P,
+                                           P, P]
         _lib = lib
     return _lib
 
@@ -119,6 +122,22 @@ def trace_lines_f64(charges, seeds, max_steps, resolution=1.0,
     if rc:
         raise RuntimeError(f"orc_trace_lines_f64 returned {rc}")
     return v, ln, cl
+
+
+def adjoint_at(charges, V, targets, resolution=1.0, curvature=True):
+    """FP64 discrete adjoint linearised at the trajectory V (3, S, n) (e.g. a
+    GPU forward's vertices): returns (L, grad (p, 4))."""
+    lib = load()
+    ch = np.ascontiguousarray(charges, np.float64)
+    V = [np.ascontiguousarray(np.asarray(V[c], np.float64).reshape(-1))
+         for c in range(3)]
+    T = [np.ascontiguousarray(np.asarray(targets[c], np.float64).reshape(-1))
+         for c in range(3)]
+    S, n = np.asarray(targets[0]).shape
+    g = np.zeros(ch.size)
+    L = lib.orc_adjoint_at_f64(_p(ch), len(ch), *map(_p, V), n, S, resolution,
+                               int(bool(curvature)), *map(_p, T), _p(g))
+    return L, g.reshape(-1, 4)
 
 
 class Frozen:

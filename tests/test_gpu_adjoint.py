@@ -14,11 +14,71 @@ def rel(a, b):
     return np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b))
 
 
-def test_adjoint_matches_fp64_discrete_adjoint(em, gpu, adjoint_case):
+@pytest.mark.parametrize("checkpoint", [False, True])
+def test_adjoint_matches_fp64_discrete_adjoint(em, gpu, adjoint_case, checkpoint):
     ch, seeds, rows, targets, fz = adjoint_case
-    out = em.adjoint(seeds, ch, rows, targets)
+    out = em.adjoint(seeds, ch, rows, targets, checkpoint=checkpoint)
     assert out["loss"] == pytest.approx(fz.L, rel=1e-4)
     assert rel(out["grad"], fz.grad()) <= GRAD_RTOL
+
+
+def _shape_case(orc, p, n=40, rows=150, seed=7):
+    """p charges in [-10,10]^3 (70 % positive, so the set's net charge is
+    positive and the lines leave the cloud), n lines seeded 35..45 from the
+    origin, rows spanning three 64-row segments and a partial 32-row
+    block."""
+    rng = np.random.default_rng(seed + p)
+    ch = np.zeros((p, 4))
+    ch[:, :3] = rng.uniform(-10, 10, (p, 3))
+    ch[:, 3] = rng.uniform(1, 10, p) * rng.choice([-1, 1], p, p=[0.3, 0.7])
+    d = rng.normal(size=(n, 3))
+    seeds = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(35, 45, (n, 1))
+    ch = ch.astype(np.float32).astype(np.float64)
+    seeds = seeds.astype(np.float32).astype(np.float64)
+    fz = orc.Frozen(ch, seeds, rows, np.zeros((3, rows, n)))
+    V = np.stack([v.reshape(rows, n) for v in fz.V])
+    targets = (V + rng.normal(0, 0.1, V.shape)).astype(np.float32)
+    fz = orc.Frozen(ch, seeds, rows, targets.astype(np.float64))
+    return ch, seeds, rows, targets, fz
+
+
+# p -> backward shape: 300 (16 charges per lane), 1000 (32 per lane, one warp
+# per line), 1500 and 3000 (two and four warps per line), 5000 (two-pass).
+# Over 150 rows the FP32 forward drifts from an FP64 forward wherever a line
+# passes near a charge, so the reference here is the FP64 discrete adjoint
+# linearised at the GPU's own trajectory: only the backward's arithmetic
+# differs.
+@pytest.mark.parametrize("p", [300, 1000, 1500, 3000, 5000])
+@pytest.mark.parametrize("checkpoint", [False, True])
+def test_adjoint_backward_shapes(em, gpu, orc, p, checkpoint):
+    ch, seeds, rows, targets, _ = _shape_case(orc, p)
+    out = em.adjoint(seeds, ch, rows, targets, checkpoint=checkpoint)
+    L, g = orc.adjoint_at(ch, out["vertices"], targets)
+    assert out["loss"] == pytest.approx(L, rel=1e-6)
+    assert rel(out["grad"], g) <= GRAD_RTOL
+    npairs = len(seeds) * (rows - 1) * p
+    passes = 3 if p > 4096 else (2 if checkpoint else 1)
+    assert out["bwd_pairs"] == pytest.approx(passes * npairs)
+
+
+def test_adjoint_stored_and_checkpoint_agree(em, gpu, orc):
+    """Both modes trace the same vertices and see the same field bits (the
+    recompute repeats the forward's order); the gradients differ only where
+    the register sums are flushed (every 512 rows, or per 64-row launch)."""
+    ch, seeds, rows, targets, _ = _shape_case(orc, 1000)
+    a = em.adjoint(seeds, ch, rows, targets, checkpoint=False)
+    b = em.adjoint(seeds, ch, rows, targets, checkpoint=True)
+    assert np.array_equal(a["vertices"], b["vertices"])
+    assert a["loss"] == b["loss"]
+    assert rel(a["grad"], b["grad"]) <= 1e-6
+
+
+def test_adjoint_repeats_bit_for_bit(em, gpu, adjoint_case):
+    """Team partials are summed in a fixed order: two calls agree exactly."""
+    ch, seeds, rows, targets, _ = adjoint_case
+    a = em.adjoint(seeds, ch, rows, targets)
+    b = em.adjoint(seeds, ch, rows, targets)
+    assert np.array_equal(a["grad"], b["grad"])
 
 
 def test_adjoint_matches_complex_step(em, gpu, adjoint_case):
