@@ -3,11 +3,13 @@
 Import with importlib (the directory name carries hyphens):
     em = importlib.import_module("electromag-with-cuda_gb300")
 """
-from . import _capi, autotune, shard, tracer, workloads  # noqa: F401
+from . import _capi, autotune, inputs, outputs, shard, tracer, workloads  # noqa: F401
 from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
 from .tracer import (adjoint, adjoint_device, calc_field, field,  # noqa: F401
                      new_lines, seed_fibonacci,
                      trace_batch, trace_lines, trace_loss_function)
 
-__all__ = ["calc_field", "field", "new_lines", "trace_lines", "seed_fibonacci", "load", "declared_symbols", "strerror",
-           "EmError", "workloads"]
+__all__ = ["calc_field", "field", "new_lines", "trace_lines", "seed_fibonacci",
+           "adjoint", "adjoint_device", "trace_batch", "trace_loss_function",
+           "load", "declared_symbols", "strerror", "EmError", "inputs",
+           "outputs", "workloads"]

@@ -91,7 +91,20 @@ _SIGNATURES = {
     "em_release": (I, []),
     "em_strerror": (ctypes.c_char_p, [I]),
     "em_version": (ctypes.c_char_p, []),
+    "em_preset": (I, [ctypes.c_char_p, P]),
+    "em_init_charges_f32": (I, [P, S, ctypes.c_uint]),
+    "em_init_charges_f64": (I, [P, S, ctypes.c_uint]),
+    "em_init_lines_f32": (I, [P, P, P, S, S, S, I, ctypes.c_uint]),
+    "em_init_lines_f64": (I, [P, P, P, S, S, S, I, ctypes.c_uint]),
+    "em_save_lines_text_f32": (I, [ctypes.c_char_p, S, S, P, P, P, P, P, P]),
+    "em_autoregress_f32": (I, [ctypes.c_char_p, S, S, P, P, P, P, P, P, F, P,
+                               P, P]),
 }
+
+
+class EmPresetParams(ctypes.Structure):
+    _fields_ = [("nx", S), ("ny", S), ("nz", S), ("p_static", S),
+                ("p_dynamic", S), ("len", S)]
 
 
 def declared_symbols():

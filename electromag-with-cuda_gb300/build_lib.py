@@ -1,4 +1,5 @@
-"""Builds libemgb300.so in-tree from csrc/*.cu for sm_103a (GB300).
+"""Builds libemgb300.so in-tree from csrc/*.cu (device code, sm_103a for
+GB300) and csrc/*.cpp (host code, no floating-point contraction).
 
 Each translation unit is compiled by its own nvcc process, in parallel, then
 linked into electromag-with-cuda_gb300/libemgb300.so (static CUDA runtime, so
@@ -40,20 +41,23 @@ def _newer(target, deps):
 
 
 def build(verbose=False, force=False):
-    """Compile every csrc/*.cu and link libemgb300.so; returns its path."""
+    """Compile every csrc/*.cu and csrc/*.cpp and link libemgb300.so; returns
+    its path."""
     nvcc = nvcc_path()
     os.makedirs(BUILD, exist_ok=True)
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) +
+                     glob.glob(os.path.join(CSRC, "*.cpp")))
     headers = sorted(glob.glob(os.path.join(CSRC, "*.h")) +
                      glob.glob(os.path.join(CSRC, "*.cuh")) +
                      glob.glob(os.path.join(ROOT, "include", "*.h")))
     objs = []
     jobs = []
     for src in sources:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(obj)
+        extra = ["-Xcompiler", "-ffp-contract=off"] if src.endswith(".cpp") else []
         if force or not _newer(obj, [src] + headers):
-            jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -401,6 +401,7 @@ const char *em_strerror(int code)
     case EM_ERR_TIMEOUT: return "device-side wait timed out";
     case EM_ERR_NO_DEVICE: return "no usable CUDA device";
     case EM_ERR_TOO_LARGE: return "size beyond this entry point's limit";
+    case EM_ERR_IO: return "file could not be opened or written";
     default: return "unknown error";
     }
 }

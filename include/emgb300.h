@@ -52,6 +52,7 @@ extern "C" {
 #define EM_ERR_TIMEOUT 12      /* a device-side wait hit its time limit    */
 #define EM_ERR_NO_DEVICE 13    /* no CUDA device / library not usable      */
 #define EM_ERR_TOO_LARGE 14    /* sizes beyond what the entry point takes  */
+#define EM_ERR_IO 15           /* a file could not be opened or written    */
 
 /* ---- arithmetic of the pair sum ------------------------------------------ */
 #define EM_ARITH_FAST 0   /* FP32 (or FP64 for _f64) rsqrt + FMA             */
@@ -280,6 +281,63 @@ EM_API int em_field_f32(const float *px, const float *py, const float *pz,
 EM_API int em_field_f64(const double *px, const double *py, const double *pz,
                         size_t m, const double *charges, size_t p, double *ex,
                         double *ey, double *ez, const em_options *opt);
+
+/* ---- the reference program's inputs and outputs (host code) --------------
+ * Presets of ElectroMag.cpp:43-55 (SimulationParams: lines nx*ny*nz, static
+ * charges, rows per line), selected there by --bogo, --micro, --enhanced,
+ * --extreme, --insane, --fuckingInsane (default "normal"; "cpu" is defined
+ * but unreachable from the command line).  Returns EM_ERR_ARG for an
+ * unknown name. */
+typedef struct em_preset_params {
+    size_t nx, ny, nz;     /* line grid                                      */
+    size_t p_static;       /* point charges                                  */
+    size_t p_dynamic;      /* unused by the tracer (0 in every preset)       */
+    size_t len;            /* rows per line, the seed row included           */
+} em_preset_params;
+EM_API int em_preset(const char *name, em_preset_params *out);
+
+/* InitializePointChargeArray ("Electromag utils.h":91-111): per charge x, y,
+ * z = (rand() - RAND_MAX/2) / RAND_MAX * 10000 and q = (rand() - RAND_MAX/10)
+ * / RAND_MAX, in the reference's T arithmetic, from the C library's rand()
+ * stream after srand(seed) (the reference: seed 1, or a timer with
+ * --randseed).  The stream is this library's own restatement of the GNU C
+ * library's additive generator, so results do not depend on the host's
+ * libc and the caller's rand() state is untouched.  charges: p {x,y,z,q}. */
+EM_API int em_init_charges_f32(float *charges, size_t p, unsigned seed);
+EM_API int em_init_charges_f64(double *charges, size_t p, unsigned seed);
+/* InitializeFieldLineArray ("Electromag utils.h":29-70) into the first
+ * nx*ny*nz entries of x, y, z (row 0 of the line arrays).  Grid mode
+ * (random = 0): 10 * (i - w/2 + 1e-5) per axis, line k*w*h + j*w + i; random
+ * mode: (rand() - RAND_MAX/2) / RAND_MAX * 10000 per component after
+ * srand(seed). */
+EM_API int em_init_lines_f32(float *x, float *y, float *z, size_t nx, size_t ny,
+                             size_t nz, int random, unsigned seed);
+EM_API int em_init_lines_f64(double *x, double *y, double *z, size_t nx,
+                             size_t ny, size_t nz, int random, unsigned seed);
+
+/* The --save dump (ElectroMag.cpp:372-397): for each line, for each row,
+ * " CPUL [line][row] x: X y: Y z: Z" from the a arrays, then the same with
+ * "GPUL" from the b arrays; either set may be NULL (the reference writes
+ * only the enabled paths).  Floats print like std::ostream's default (%g,
+ * six significant digits).  Host pointers, reference layout (row*n + line). */
+EM_API int em_save_lines_text_f32(const char *path, size_t n, size_t rows,
+                                  const float *ax, const float *ay,
+                                  const float *az, const float *bx,
+                                  const float *by, const float *bz);
+/* The --autoregress check (ElectroMag.cpp:400-453): per line, the first row
+ * where |a - b| (FP32, the reference's vec3Len(vec3(a, b))) exceeds
+ * threshold (the reference: 0.1).  first[line] gets that row or -1; when
+ * path is not NULL the report is written in the reference's regression.txt
+ * format (the previous row, the diverging row, their 3D offsets; row 0 is
+ * reported alone).  *ndiverged (optional) counts the lines that diverge.
+ * The scan runs on the GPU; with opt->device_ptrs all six arrays are device
+ * pointers, else host arrays that are copied in.  first may be NULL. */
+EM_API int em_autoregress_f32(const char *path, size_t n, size_t rows,
+                              const float *ax, const float *ay,
+                              const float *az, const float *bx,
+                              const float *by, const float *bz,
+                              float threshold, long long *first,
+                              size_t *ndiverged, const em_options *opt);
 
 /* Library state.  em_device_count: CUDA devices visible (0 when none).
  * em_release: frees the cached device buffers of the current device.

@@ -1,9 +1,11 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE: builds the reference's own CPU tracer from its sources
 # where they lie (read-only) into oracle/_ref/.  Nothing is copied from the
-# reference tree.  Two variants:
+# reference tree.  Variants:
 #   libemref_strict.so  -O3 -msse2 -fopenmp, IEEE arithmetic (no fast-math)
 #   libemref_fast.so    the reference's release flags (CMakeLists.txt:24)
+#   libemref_generic.so the scalar templates (no __SSE__)
+#   libemref_inputs.so  the input generators of "Electromag utils.h"
 # The reference's x86 path uses SSE intrinsics; on other architectures it
 # falls back to the generic template (CPU_Implement.cpp:104-191) and the
 # -msse2/-mfpmath flags do not exist, so they are only passed on x86.
@@ -31,4 +33,7 @@ g++ $COMMON $ARCHFLAGS -ffast-math -fno-math-errno -ffinite-math-only \
 # x86 too, with the same IEEE scalar arithmetic.
 g++ $COMMON $ARCHFLAGS -U__SSE__ "$SRC" "$HERE/ref_shim.cpp" \
     -o "$OUT/libemref_generic.so"
-echo "built $OUT/libemref_{strict,fast,generic}.so ($(uname -m))"
+# The reference's input generators ("Electromag utils.h":29-111), header
+# templates, with the C library's rand().
+g++ $COMMON $ARCHFLAGS "$HERE/ref_inputs_shim.cpp" -o "$OUT/libemref_inputs.so"
+echo "built $OUT/libemref_{strict,fast,generic,inputs}.so ($(uname -m))"

@@ -133,6 +133,23 @@ def main():
     seeds = np.concatenate([seeds, np.repeat(seeds[:1], n - len(seeds), 0)])
     add("cfg_cpu_2500", "f32", seeds, ch, n, 2500, 1.0, 1, ["strict"],
         rows=[0, 1, 2, 5, 10, 50, 100, 250, 500, 1000, 2000, 2499])
+    # the reference program's own runs: --bogo (16x16 grid, 50 charges, 500
+    # rows) and the default preset (128x128 grid, 1024 charges, 2500 rows),
+    # inputs from its generators (InitializePointChargeArray with srand(1),
+    # InitializeFieldLineArray grid mode) through oracle/_ref/libemref_inputs.so
+    inp = ctypes.CDLL(os.path.join(REFDIR, "libemref_inputs.so"))
+    inp.ref_init_charges_f32.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    inp.ref_init_grid_f32.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_size_t] * 3
+    for name, (w, h, p, rows, sample) in {
+            "preset_bogo": (16, 16, 50, 500, [0, 1, 2, 10, 100, 250, 499]),
+            "preset_normal": (128, 128, 1024, 2500, [1, 1000, 2499])}.items():
+        ch = np.zeros((p, 4), np.float32)
+        inp.ref_init_charges_f32(ch.ctypes.data, p)
+        g = np.zeros((3, w * h), np.float32)
+        inp.ref_init_grid_f32(g[0].ctypes.data, g[1].ctypes.data,
+                              g[2].ctypes.data, w, h, 1)
+        add(name, "f32", g.T.copy(), ch, w * h, rows, 1.0, 1, ["strict"],
+            rows=sample)
     # error codes: n == 0, resolution == 0, total_steps < 2, n % 64 != 0
     ch = charges_uniform(rng, 4, 50.0, np.float32)
     seeds = rng.uniform(-60, 60, (64, 3)).astype(np.float32)
