@@ -522,8 +522,86 @@ def batch_block(em, torch, dev, seed):
             "speedup_vs_per_set_wall": wall / bt}
 
 
+def reference_run_block(em, torch, dev, seed):
+    """The reference program's own default run (preset "normal": srand(1)
+    charges, 128x128 grid seeds, 1024 charges, 2500 rows; ElectroMag.cpp:43,
+    251-266): GPU with the reference's arithmetic (bit-exact) and the fast
+    arithmetic, the oracle port on host cores over a line sample, the
+    --autoregress scan of the two GPU runs and the --save dump of a preset
+    run."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import em_oracle as orc
+    ch, seeds, rows = em.inputs.reference_case("normal")
+    n, p = len(seeds), len(ch)
+    pairs = float(n) * (rows - 1) * p
+    blk = {"workload": "preset_normal", "lines": n, "charges": p, "rows": rows}
+    runs = {}
+    chd = torch.from_numpy(ch).to(dev)
+    for arith in ("exact", "fast"):
+        V = torch.zeros((3, rows, n), dtype=torch.float32, device=dev)
+        V[:, 0, :] = torch.from_numpy(seeds.T.copy()).to(dev)
+        times = []
+        for rep in range(2):
+            W = V.clone()
+            rc, perf = em.calc_field(W[0].reshape(-1), W[1].reshape(-1),
+                                     W[2].reshape(-1), chd, n, 1.0, True,
+                                     arith=arith)
+            if rc:
+                raise em.EmError(rc, f"preset run ({arith})")
+            times.append(perf.time)
+        runs[arith] = W
+        blk[arith] = {"ms": min(times) * 1e3,
+                      "gpair_s": pairs / min(times) / 1e9}
+    threads = os.cpu_count() or 1
+    rate, sample = cpu_rate(orc, ch, seeds, rows, 10.0, threads)
+    blk["cpu_port"] = {"gpair_s": rate, "cores": threads,
+                       "full_run_s_estimate": pairs / rate / 1e9,
+                       "sample": f"{sample['lines']} lines x {p} charges x "
+                                 f"{sample['rows']} rows"}
+    # --autoregress: exact against fast, then a run against itself (no
+    # divergence: every vertex of both runs read once)
+    stream = torch.cuda.current_stream(dev)
+    for name, b in (("exact_vs_fast", runs["fast"]), ("identical", runs["exact"])):
+        em.outputs.autoregress(runs["exact"], b)  # warm-up
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        first, count = em.outputs.autoregress(runs["exact"], b)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        rows_read = np.where(first >= 0, first + 1, rows).sum()
+        gbytes = float(rows_read) * 24 / 1e9
+        blk["autoregress_" + name] = {
+            "ms": ms, "diverged_lines": count,
+            "median_first_row": float(np.median(first[first >= 0])) if count else None,
+            "algorithmic_gb": gbytes, "gb_s": gbytes / (ms * 1e-3)}
+    # --save: the bogo preset's run (256 lines x 500 rows), both tags
+    bch, bseeds, brows = em.inputs.reference_case("bogo")
+    bn = len(bseeds)
+    V = np.zeros((3, brows, bn), np.float32)
+    V[:, 0, :] = bseeds.T
+    rc, _ = em.calc_field(V[0].reshape(-1), V[1].reshape(-1), V[2].reshape(-1),
+                          bch, bn, 1.0, True, arith="exact")
+    if rc:
+        raise em.EmError(rc, "bogo run")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "data.txt")
+        t = time.perf_counter()
+        em.outputs.save_lines(path, bn, brows, V, V)
+        sec = time.perf_counter() - t
+        size = os.path.getsize(path)
+    blk["save_bogo"] = {"seconds": sec, "mbytes": size / 1e6,
+                        "mb_s": size / 1e6 / sec, "threads": threads}
+    del runs
+    torch.cuda.empty_cache()
+    return blk
+
+
 def run_extras(em, torch, dev, args):
     out = {}
+    out["reference_run"] = reference_run_block(em, torch, dev, args.seed)
     out["batched"] = batch_block(em, torch, dev, args.seed)
     out["precision"] = precision_block(em, torch, dev, args.workload, 5000,
                                        args.seed, 20000, True)

@@ -207,9 +207,11 @@ int em_save_lines_text_f32(const char *path, size_t n, size_t rows, const float 
         return EM_ERR_IO;
     // lines are formatted by all host threads in blocks and written in order
     const unsigned nt = std::max(1u, std::thread::hardware_concurrency());
-    // about 8 MB of text per thread and block (a dump line is ~60 bytes)
+    // at most about 8 MB of text per thread and block (a dump line is ~60
+    // bytes), and every thread busy when the lines run out sooner
     const size_t line_bytes = (rows ? rows : 1) * 60 * ((a ? 1 : 0) + (b ? 1 : 0));
-    const size_t per_block = std::max<size_t>(1, (size_t(8) << 20) / line_bytes);
+    const size_t per_block = std::max<size_t>(
+        1, std::min((size_t(8) << 20) / line_bytes, (n + nt - 1) / nt));
     std::vector<std::string> part(nt);
     bool ok = true;
     for (size_t l0 = 0; l0 < n && ok; l0 += per_block * nt) {

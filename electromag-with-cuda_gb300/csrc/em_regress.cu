@@ -57,11 +57,28 @@ __global__ void __launch_bounds__(256) diverge_kernel(const RegressArgs A)
         const int s1 = min(A.rows, s0 + kRegressChunk);
         if (*(volatile unsigned long long *)(A.first + line) <= (unsigned long long)s0)
             continue; // an earlier chunk already found this line's row
-        for (int s = s0; s < s1; ++s) {
-            const size_t i = (size_t)s * (size_t)A.n + (size_t)line;
-            if (offset3(A.ax[i], A.ay[i], A.az[i], A.bx[i], A.by[i], A.bz[i]) > A.thr) {
-                atomicMin(A.first + line, (unsigned long long)s);
-                break;
+        // four rows' loads in flight before their offsets are tested
+        constexpr int U = 4;
+        bool found = false;
+        for (int s = s0; s < s1 && !found; s += U) {
+            float v[U][6];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const size_t i = (size_t)min(s + u, s1 - 1) * (size_t)A.n + (size_t)line;
+                v[u][0] = A.ax[i];
+                v[u][1] = A.ay[i];
+                v[u][2] = A.az[i];
+                v[u][3] = A.bx[i];
+                v[u][4] = A.by[i];
+                v[u][5] = A.bz[i];
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (!found && s + u < s1 &&
+                    offset3(v[u][0], v[u][1], v[u][2], v[u][3], v[u][4], v[u][5]) > A.thr) {
+                    atomicMin(A.first + line, (unsigned long long)(s + u));
+                    found = true;
+                }
             }
         }
     }
