@@ -5,7 +5,8 @@ Import with importlib (the directory name carries hyphens):
 """
 from . import _capi, autotune, inputs, outputs, shard, tracer, workloads  # noqa: F401
 from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
-from .tracer import (adjoint, adjoint_device, calc_field, field,  # noqa: F401
+from .tracer import (adjoint, adjoint_device, calc_field, calc_field_multi,  # noqa: F401
+                     field,
                      new_lines, seed_fibonacci,
                      trace_batch, trace_lines, trace_loss_function)
 

@@ -91,6 +91,13 @@ _SIGNATURES = {
     "em_release": (I, []),
     "em_strerror": (ctypes.c_char_p, [I]),
     "em_version": (ctypes.c_char_p, []),
+    "em_calc_field_part_f32": (I, [I, P, P, P, S, S, S, S, P, S, F, I, P, P]),
+    "em_calc_field_part_f64": (I, [I, P, P, P, S, S, S, S, P, S, D, I, P, P]),
+    "em_calc_field_multi_f32": (I, [P, S, P, P, P, S, S, P, S, F, I, P, P, P,
+                                    P]),
+    "em_calc_field_multi_f64": (I, [P, S, P, P, P, S, S, P, S, D, I, P, P, P,
+                                    P]),
+    "em_release_device": (I, [I]),
     "em_preset": (I, [ctypes.c_char_p, P]),
     "em_init_charges_f32": (I, [P, S, ctypes.c_uint]),
     "em_init_charges_f64": (I, [P, S, ctypes.c_uint]),

@@ -106,10 +106,13 @@ int read_dev_err(DevCtx &c, cudaStream_t s, int *dev_err_host)
 
 namespace {
 
+// Traces lines [line0, line0 + nl) of the caller's arrays (n lines per row;
+// nl = n: all of them).  A partial range needs host arrays: its row-0 seeds
+// go in as one contiguous slice and rows 1.. come back as a pitched copy.
 template <class T>
 int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges, size_t p,
                T resolution, int use_curvature, const em_options *opt, bool plain,
-               em_perf *perf)
+               em_perf *perf, size_t line0 = 0, size_t nl = 0)
 {
     using clock = std::chrono::steady_clock;
     const auto t_start = clock::now();
@@ -137,6 +140,10 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         return EM_ERR_TOO_LARGE;
     if (o.device_ptrs && ((uintptr_t)charges & 15))
         return EM_ERR_ARG;
+    if (!nl)
+        nl = n;
+    if (line0 > n || nl > n - line0 || (nl != n && o.device_ptrs))
+        return EM_ERR_ARG;
     if (perf)
         perf->progress = 0;
 
@@ -148,7 +155,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     std::lock_guard<std::mutex> guard(c.mu);
 
     Plan pl;
-    code = make_plan<T>(c, n, p, o, &pl);
+    code = make_plan<T>(c, nl, p, o, &pl);
     if (code)
         return code;
     const size_t rec = sizeof(T) * 4;
@@ -163,7 +170,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     c.err = static_cast<int *>(c.errbuf);
 
     T *dx = x, *dy = y, *dz = z;
-    const size_t elems = n * total_steps;
+    const size_t elems = nl * total_steps;
     if (!o.device_ptrs) {
         if ((code = grow(&c.lines, &c.lines_cap, 3 * elems * sizeof(T))))
             return code;
@@ -181,11 +188,11 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     if (e == cudaSuccess)
         e = cudaMemsetAsync(c.err, 0, sizeof(int), s);
     if (e == cudaSuccess && !o.device_ptrs) {
-        e = cudaMemcpyAsync(dx, x, n * sizeof(T), cudaMemcpyHostToDevice, s);
+        e = cudaMemcpyAsync(dx, x + line0, nl * sizeof(T), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(dy, y, n * sizeof(T), cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(dy, y + line0, nl * sizeof(T), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(dz, z, n * sizeof(T), cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(dz, z + line0, nl * sizeof(T), cudaMemcpyHostToDevice, s);
     }
     if (e != cudaSuccess)
         return map_cuda(e);
@@ -195,7 +202,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     prm.y = dy;
     prm.z = dz;
     prm.charges = c.charges;
-    prm.n = (long long)n;
+    prm.n = (long long)nl;
     prm.n_groups = pl.n_groups;
     prm.total_steps = (int)total_steps;
     prm.p_pad = pl.p_pad;
@@ -214,13 +221,23 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         e = cudaEventRecord(c.ev1, s);
     if (e != cudaSuccess)
         return map_cuda(e);
-    if (!o.device_ptrs) {
+    if (!o.device_ptrs && nl == n) {
         const size_t rest = elems - n;
         e = cudaMemcpyAsync(x + n, dx + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(y + n, dy + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(z + n, dz + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess)
+            return map_cuda(e);
+    } else if (!o.device_ptrs) {
+        // rows 1.. of the range: nl values per row into a row pitch of n
+        T *dst[3] = {x, y, z};
+        const T *src[3] = {dx, dy, dz};
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+            e = cudaMemcpy2DAsync(dst[k] + n + line0, n * sizeof(T), src[k] + nl,
+                                  nl * sizeof(T), nl * sizeof(T), total_steps - 1,
+                                  cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess)
             return map_cuda(e);
     }
@@ -233,9 +250,9 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     if (perf) {
         const double tk = ms * 1e-3;
         perf->time = tk;
-        perf->pairs = (double)n * (double)(total_steps - 1) * (double)p;
+        perf->pairs = (double)nl * (double)(total_steps - 1) * (double)p;
         perf->performance =
-            tk > 0 ? (double)n * (double)(total_steps - 1) * (18.0 * (double)p + 13.0) / tk / 1e9
+            tk > 0 ? (double)nl * (double)(total_steps - 1) * (18.0 * (double)p + 13.0) / tk / 1e9
                    : 0;
         perf->wall_time = std::chrono::duration<double>(clock::now() - t_start).count();
         perf->progress = 1.0;
@@ -322,6 +339,61 @@ int em_field_f64(const double *px, const double *py, const double *pz, size_t m,
     return em::field_at<double>(px, py, pz, m, charges, p, ex, ey, ez, opt);
 }
 
+} // extern "C"
+
+namespace em {
+namespace {
+
+// Runs one line range on `device` from whichever host thread calls it; the
+// caller's current device is restored afterwards.
+template <class T>
+int calc_field_part(int device, T *x, T *y, T *z, size_t n, size_t total_steps, size_t line0,
+                    size_t nlines, const T *charges, size_t p, T resolution, int use_curvature,
+                    const em_options *opt, em_perf *perf)
+{
+    if (!nlines)
+        return EM_ERR_N_ZERO;
+    if (opt && opt->device_ptrs)
+        return EM_ERR_ARG;
+    int ndev = 0, prev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return EM_ERR_NO_DEVICE;
+    }
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_NO_DEVICE;
+    }
+    const int code = calc_field<T>(x, y, z, n, total_steps, charges, p, resolution,
+                                   use_curvature, opt, false, perf, line0, nlines);
+    cudaSetDevice(prev);
+    return code;
+}
+
+} // namespace
+} // namespace em
+
+extern "C" {
+
+int em_calc_field_part_f32(int device, float *x, float *y, float *z, size_t n,
+                           size_t total_steps, size_t line0, size_t nlines,
+                           const float *charges, size_t p, float resolution, int use_curvature,
+                           const em_options *opt, em_perf *perf)
+{
+    return em::calc_field_part<float>(device, x, y, z, n, total_steps, line0, nlines, charges,
+                                      p, resolution, use_curvature, opt, perf);
+}
+
+int em_calc_field_part_f64(int device, double *x, double *y, double *z, size_t n,
+                           size_t total_steps, size_t line0, size_t nlines,
+                           const double *charges, size_t p, double resolution,
+                           int use_curvature, const em_options *opt, em_perf *perf)
+{
+    return em::calc_field_part<double>(device, x, y, z, n, total_steps, line0, nlines, charges,
+                                       p, resolution, use_curvature, opt, perf);
+}
+
 int em_calc_field_f32(float *x, float *y, float *z, size_t n, size_t total_steps,
                       const float *charges, size_t p, float resolution, int use_curvature,
                       em_perf *perf)
@@ -362,6 +434,23 @@ int em_device_count(void)
         return 0;
     }
     return n;
+}
+
+int em_release_device(int device)
+{
+    int prev = 0, ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return EM_ERR_NO_DEVICE;
+    }
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_NO_DEVICE;
+    }
+    const int code = em_release();
+    cudaSetDevice(prev);
+    return code;
 }
 
 int em_release(void)

@@ -9,6 +9,8 @@ writes rows 1..total_steps-1 in place.  numpy arrays go through the
 host-pointer entry points; CUDA torch tensors through the device-pointer ones
 on the current torch stream.
 """
+import ctypes
+
 import numpy as np
 
 from . import _capi
@@ -349,6 +351,36 @@ def adjoint_device(V, charges, targets, resolution=1.0, use_curvature=True,
     if rc:
         raise _capi.EmError(rc, "em_adjoint_f32")
     return loss, grad, fwd.time, bwd.time
+
+
+def calc_field_multi(x, y, z, charges, n, devices, resolution=1.0,
+                     use_curvature=True, *, arith="fast", rule="sse",
+                     threads_per_line=0, lines_per_thread=0):
+    """The trace split over CUDA devices (em_calc_field_multi_*): one line
+    range per entry of `devices` (ordinals may repeat), one host thread per
+    range, failed ranges moved to devices that succeeded.  Host arrays in
+    the reference layout.  Returns (rc, perf, ran_on list, nfailed)."""
+    lib = _capi.load()
+    f32 = str(x.dtype).endswith("float32")
+    for a in (x, y, z, charges):
+        _check(a, "float32" if f32 else "float64")
+    steps = x.size // n if n else 0
+    p = charges.size // 4
+    o = _capi.EmOptions()
+    o.arith = _ARITH[arith]
+    o.rule = _RULE[rule]
+    o.threads_per_line = threads_per_line
+    o.lines_per_thread = lines_per_thread
+    devs = np.ascontiguousarray(devices, np.int32)
+    ran = np.full(len(devs), -1, np.int32)
+    nfailed = ctypes.c_size_t(0)
+    perf = _capi.EmPerf()
+    fn = lib.em_calc_field_multi_f32 if f32 else lib.em_calc_field_multi_f64
+    rc = fn(devs.ctypes.data, len(devs), _ptr(x), _ptr(y), _ptr(z), n, steps,
+            _ptr(charges), p, resolution, int(bool(use_curvature)),
+            ctypes_byref(o), ctypes_byref(perf), ctypes_byref(nfailed),
+            ran.ctypes.data)
+    return rc, perf, ran.tolist(), int(nfailed.value)
 
 
 def trace_batch(sets, max_steps, resolution=1.0, term_radius=0.5, *,

@@ -282,6 +282,48 @@ EM_API int em_field_f64(const double *px, const double *py, const double *pz,
                         size_t m, const double *charges, size_t p, double *ex,
                         double *ey, double *ez, const em_options *opt);
 
+/* One range of lines, [line0, line0 + nlines), of the caller's host arrays
+ * (reference layout, n lines per row) traced on CUDA device `device`, from
+ * any host thread (the calling thread's current device is restored).  Row 0
+ * of the range is read, rows 1..total_steps-1 of the range are written; the
+ * rest of the arrays is untouched, so ranges on different devices may run
+ * at the same time.  The per-device work of the reference's multi-device
+ * functor (GPGPU_Segment/src/Abstract_Functor.cpp:29-160, MainFunctor of
+ * ElectrostaticFunctor.hpp) with the rule and codes of em_calc_field_ex_*;
+ * EM_ERR_NO_DEVICE for a device that does not exist.  Host pointers only. */
+EM_API int em_calc_field_part_f32(int device, float *x, float *y, float *z,
+                                  size_t n, size_t total_steps, size_t line0,
+                                  size_t nlines, const float *charges, size_t p,
+                                  float resolution, int use_curvature,
+                                  const em_options *opt, em_perf *perf);
+EM_API int em_calc_field_part_f64(int device, double *x, double *y, double *z,
+                                  size_t n, size_t total_steps, size_t line0,
+                                  size_t nlines, const double *charges,
+                                  size_t p, double resolution, int use_curvature,
+                                  const em_options *opt, em_perf *perf);
+
+/* The whole trace split over several CUDA devices by the functor of
+ * include/emgb300_functor.hpp (the reference's AbstractFunctor lifecycle
+ * and remap policy, Abstract_Functor.cpp:29-160): one contiguous range of
+ * lines per entry of devices[] (an ordinal may repeat), one host thread per
+ * range; a range whose device fails moves to a device that has succeeded.
+ * ran_on (optional, ndevices entries) gets the device each range completed
+ * on, -1 if none; *nfailed (optional) the ranges that never completed.
+ * Returns EM_OK when every range completed, else the last failing range's
+ * code.  Host pointers only. */
+EM_API int em_calc_field_multi_f32(const int *devices, size_t ndevices, float *x,
+                                   float *y, float *z, size_t n,
+                                   size_t total_steps, const float *charges,
+                                   size_t p, float resolution, int use_curvature,
+                                   const em_options *opt, em_perf *perf,
+                                   size_t *nfailed, int *ran_on);
+EM_API int em_calc_field_multi_f64(const int *devices, size_t ndevices,
+                                   double *x, double *y, double *z, size_t n,
+                                   size_t total_steps, const double *charges,
+                                   size_t p, double resolution,
+                                   int use_curvature, const em_options *opt,
+                                   em_perf *perf, size_t *nfailed, int *ran_on);
+
 /* ---- the reference program's inputs and outputs (host code) --------------
  * Presets of ElectroMag.cpp:43-55 (SimulationParams: lines nx*ny*nz, static
  * charges, rows per line), selected there by --bogo, --micro, --enhanced,
@@ -344,6 +386,8 @@ EM_API int em_autoregress_f32(const char *path, size_t n, size_t rows,
  * em_strerror: text for a return code. */
 EM_API int em_device_count(void);
 EM_API int em_release(void);
+/* em_release for one device ordinal (the calling thread's device is kept). */
+EM_API int em_release_device(int device);
 EM_API const char *em_strerror(int code);
 /* Diagnostics.  em_fp32_peak_tflops: measured FP32 FFMA throughput of the
  * current device (dense FMA chains, 2 FLOP per FMA), the denominator of the
