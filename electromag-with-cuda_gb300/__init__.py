@@ -8,7 +8,8 @@ from ._capi import EmError, load, declared_symbols, strerror  # noqa: F401
 from .tracer import (adjoint, adjoint_device, calc_field, calc_field_multi,  # noqa: F401
                      field,
                      new_lines, seed_fibonacci,
-                     trace_batch, trace_lines, trace_loss_function)
+                     trace_batch, trace_lines, trace_loss_function,
+                     verlet_step)
 
 __all__ = ["calc_field", "field", "new_lines", "trace_lines", "seed_fibonacci",
            "adjoint", "adjoint_device", "trace_batch", "trace_loss_function",

@@ -98,6 +98,8 @@ _SIGNATURES = {
     "em_calc_field_multi_f64": (I, [P, S, P, P, P, S, S, P, S, D, I, P, P, P,
                                     P]),
     "em_release_device": (I, [I]),
+    "em_verlet_step_f32": (I, [P, P, S, P, S, P, P, F, S, P, P]),
+    "em_verlet_step_f64": (I, [P, P, S, P, S, P, P, D, S, P, P]),
     "em_preset": (I, [ctypes.c_char_p, P]),
     "em_init_charges_f32": (I, [P, S, ctypes.c_uint]),
     "em_init_charges_f64": (I, [P, S, ctypes.c_uint]),

@@ -1,0 +1,300 @@
+// One velocity-Verlet step of moving point charges in the field of the
+// static charges and of each other (emgVerletStep, ElectroMag/src/
+// Particle_System.cpp:109-190, with BoundToBox :28-66 and emgFieldsAdd
+// :72-102).  The reference never instantiates it (magneto_k is defined with
+// a trailing semicolon, Magnetics.h:25, and Vector3 has no arithmetic
+// operators) and drops the updated particle; this is the step it describes:
+//
+//   v' = v + a dt/2,  r' = r + v' dt
+//   E  = K sum_static q r/|r|^3 + K sum_{j != i} q_j r/|r|^3   (r = r' - c_j)
+//   B  = magneto_k sum_{j != i} q_j v_j x r/|r|^3
+//   a'' = (q E + q v' x B) / m,  v'' = v' + a'' dt/2,  then reflection off
+//   the box walls (position mirrored, velocity component negated)
+//
+// Every particle sees the others' start-of-step states, exactly as the
+// reference's loop does (it reads dynCharges[j], which it never updates), so
+// particles are independent: one thread per particle, charges and particles
+// staged through shared memory in tiles (the all-pairs pattern of the field
+// tracer).  The tile that holds a thread's own particle runs the loop that
+// skips j = i; every other tile runs without the test.
+#include <chrono>
+#include <climits>
+#include <cstdint>
+#include <mutex>
+
+#include "em_device.cuh"
+#include "em_internal.h"
+#include "em_math.cuh"
+#include "em_plan.h"
+#include "emgb300.h"
+
+namespace em {
+namespace {
+
+constexpr double kMagnetoK = 1E-7; // magneto_k, include/Magnetics.h:25
+constexpr int kVerletBlock = 128;
+
+template <class T> struct alignas(sizeof(T) * 4) Dyn {
+    T x, y, z, q, vx, vy, vz, m; // dynamicPointCharge<T> (Electrodynamics.h:29-34)
+};
+
+template <class T> __device__ __forceinline__ T inv_len3(T r2);
+template <> __device__ __forceinline__ float inv_len3<float>(float r2)
+{
+    const float inv = rsqrt_fast(r2);
+    return inv * inv * inv;
+}
+template <> __device__ __forceinline__ double inv_len3<double>(double r2)
+{
+    const double inv = 1.0 / sqrt(r2);
+    return inv * inv * inv;
+}
+
+template <class T> struct VerletArgs {
+    const Dyn<T> *in;
+    Dyn<T> *out;
+    T *accel;            // n * 3, a(t) in, a(t + dt) out
+    const T *charges;    // p * 4 static
+    long long n;
+    int p;
+    T lo[3], hi[3];
+    T dt;
+};
+
+template <class T, bool SELF>
+__device__ __forceinline__ void dyn_tile(const Dyn<T> *tile, int count, int self, T rx, T ry,
+                                         T rz, T &ex, T &ey, T &ez, T &bx, T &by, T &bz)
+{
+#pragma unroll 4
+    for (int j = 0; j < count; ++j) {
+        if (SELF && j == self)
+            continue;
+        const Dyn<T> d = tile[j];
+        const T dx = rx - d.x, dy = ry - d.y, dz = rz - d.z;
+        const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+        const T w = d.q * inv_len3<T>(r2);
+        ex = fma(w, dx, ex);
+        ey = fma(w, dy, ey);
+        ez = fma(w, dz, ez);
+        // v_j x r
+        const T cx = fma(d.vy, dz, -d.vz * dy);
+        const T cy = fma(d.vz, dx, -d.vx * dz);
+        const T cz = fma(d.vx, dy, -d.vy * dx);
+        bx = fma(w, cx, bx);
+        by = fma(w, cy, by);
+        bz = fma(w, cz, bz);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kVerletBlock) verlet_kernel(const VerletArgs<T> A)
+{
+    __shared__ Dyn<T> dtile[kVerletBlock];
+    __shared__ T stile[kVerletBlock * 4];
+    const long long i = blockIdx.x * (long long)kVerletBlock + threadIdx.x;
+    const bool own = i < A.n;
+    Dyn<T> me{};
+    T ax = 0, ay = 0, az = 0;
+    if (own) {
+        me = A.in[i];
+        ax = A.accel[3 * i];
+        ay = A.accel[3 * i + 1];
+        az = A.accel[3 * i + 2];
+    }
+    const T dt2 = A.dt / T(2);
+    // v(t + dt/2) = v(t) + a(t) dt/2;  r(t + dt) = r(t) + v(t + dt/2) dt
+    T vx = me.vx + ax * dt2, vy = me.vy + ay * dt2, vz = me.vz + az * dt2;
+    T rx = me.x + vx * A.dt, ry = me.y + vy * A.dt, rz = me.z + vz * A.dt;
+
+    T ex = 0, ey = 0, ez = 0, bx = 0, by = 0, bz = 0;
+    for (int t0 = 0; t0 < A.p; t0 += kVerletBlock) {
+        const int cnt = min(kVerletBlock, A.p - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt * 4; k += kVerletBlock)
+            stile[k] = A.charges[4 * (size_t)t0 + k];
+        __syncthreads();
+#pragma unroll 4
+        for (int j = 0; j < cnt; ++j) {
+            const T dx = rx - stile[4 * j], dy = ry - stile[4 * j + 1],
+                    dz = rz - stile[4 * j + 2];
+            const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+            const T w = stile[4 * j + 3] * inv_len3<T>(r2);
+            ex = fma(w, dx, ex);
+            ey = fma(w, dy, ey);
+            ez = fma(w, dz, ez);
+        }
+    }
+    for (long long t0 = 0; t0 < A.n; t0 += kVerletBlock) {
+        const int cnt = (int)min((long long)kVerletBlock, A.n - t0);
+        __syncthreads();
+        if (threadIdx.x < cnt)
+            dtile[threadIdx.x] = A.in[t0 + threadIdx.x];
+        __syncthreads();
+        if (t0 == blockIdx.x * (long long)kVerletBlock)
+            dyn_tile<T, true>(dtile, cnt, threadIdx.x, rx, ry, rz, ex, ey, ez, bx, by, bz);
+        else
+            dyn_tile<T, false>(dtile, cnt, -1, rx, ry, rz, ex, ey, ez, bx, by, bz);
+    }
+    if (!own)
+        return;
+    const T K = (T)kElectroK, MK = (T)kMagnetoK;
+    ex *= K;
+    ey *= K;
+    ez *= K;
+    bx *= MK;
+    by *= MK;
+    bz *= MK;
+    // a = (q E + q v x B) / m
+    const T fx = me.q * ex + me.q * (vy * bz - vz * by);
+    const T fy = me.q * ey + me.q * (vz * bx - vx * bz);
+    const T fz = me.q * ez + me.q * (vx * by - vy * bx);
+    ax = fx / me.m;
+    ay = fy / me.m;
+    az = fz / me.m;
+    vx += ax * dt2;
+    vy += ay * dt2;
+    vz += az * dt2;
+    // BoundToBox (Particle_System.cpp:28-66): upper walls, then lower walls
+    T *r[3] = {&rx, &ry, &rz}, *v[3] = {&vx, &vy, &vz};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (*r[c] > A.hi[c]) {
+            *r[c] = T(2) * A.hi[c] - *r[c];
+            *v[c] = -*v[c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (*r[c] < A.lo[c]) {
+            *r[c] = T(2) * A.lo[c] - *r[c];
+            *v[c] = -*v[c];
+        }
+    }
+    Dyn<T> o = me;
+    o.x = rx;
+    o.y = ry;
+    o.z = rz;
+    o.vx = vx;
+    o.vy = vy;
+    o.vz = vz;
+    A.out[i] = o;
+    A.accel[3 * i] = ax;
+    A.accel[3 * i + 1] = ay;
+    A.accel[3 * i + 2] = az;
+}
+
+template <class T>
+int verlet(T *dyn, T *accel, size_t n, const T *charges, size_t p, const T *box_min,
+           const T *box_max, T dt, size_t steps, const em_options *opt, em_perf *perf)
+{
+    using clock = std::chrono::steady_clock;
+    const auto t_start = clock::now();
+    if (!n)
+        return 1; // emgVerletStep's only check
+    if (!dyn || !accel || (p && !charges) || !box_min || !box_max || !steps)
+        return EM_ERR_ARG;
+    if (n > (size_t)(LLONG_MAX / 64) || p > (size_t)INT_MAX / 4)
+        return EM_ERR_TOO_LARGE;
+    em_options o{};
+    if (opt)
+        o = *opt;
+    if (o.device_ptrs && (((uintptr_t)dyn % alignof(Dyn<T>)) ||
+                          (((uintptr_t)accel | (uintptr_t)charges) % sizeof(T))))
+        return EM_ERR_ARG;
+    int code = EM_OK;
+    DevCtx *cp = get_ctx(&code);
+    if (!cp)
+        return code;
+    DevCtx &c = *cp;
+    std::lock_guard<std::mutex> guard(c.mu);
+    cudaStream_t s = (o.device_ptrs && o.stream) ? (cudaStream_t)o.stream : c.stream;
+    const size_t dbytes = n * sizeof(Dyn<T>), abytes = n * 3 * sizeof(T);
+    const size_t cbytes = p * 4 * sizeof(T);
+    // scratch: two particle buffers (ping-pong); host calls also stage the
+    // accelerations and the charges
+    const size_t off_acc = 2 * ((dbytes + 255) / 256 * 256);
+    const size_t off_ch = off_acc + (abytes + 255) / 256 * 256;
+    if ((code = grow(&c.scratch, &c.scratch_cap, off_ch + cbytes + 256)))
+        return code;
+    unsigned char *ws = static_cast<unsigned char *>(c.scratch);
+    Dyn<T> *buf[2] = {reinterpret_cast<Dyn<T> *>(ws),
+                      reinterpret_cast<Dyn<T> *>(ws + off_acc / 2)};
+    T *dacc = accel;
+    const T *dch = charges;
+    cudaError_t e = cudaSuccess;
+    const cudaMemcpyKind kin = o.device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    e = cudaMemcpyAsync(buf[0], dyn, dbytes, kin, s);
+    if (!o.device_ptrs) {
+        dacc = reinterpret_cast<T *>(ws + off_acc);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dacc, accel, abytes, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && p) {
+            T *hc = reinterpret_cast<T *>(ws + off_ch);
+            e = cudaMemcpyAsync(hc, charges, cbytes, cudaMemcpyHostToDevice, s);
+            dch = hc;
+        }
+    }
+    VerletArgs<T> A{};
+    A.accel = dacc;
+    A.charges = dch;
+    A.n = (long long)n;
+    A.p = (int)p;
+    for (int k = 0; k < 3; ++k) {
+        A.lo[k] = box_min[k];
+        A.hi[k] = box_max[k];
+    }
+    A.dt = dt;
+    const unsigned grid = (unsigned)((n + kVerletBlock - 1) / kVerletBlock);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(c.ev0, s);
+    for (size_t k = 0; k < steps && e == cudaSuccess; ++k) {
+        A.in = buf[k & 1];
+        A.out = buf[(k + 1) & 1];
+        verlet_kernel<T><<<grid, kVerletBlock, 0, s>>>(A);
+        count_launch(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaEventRecord(c.ev1, s);
+    const cudaMemcpyKind kout = o.device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dyn, buf[steps & 1], dbytes, kout, s);
+    if (e == cudaSuccess && !o.device_ptrs)
+        e = cudaMemcpyAsync(accel, dacc, abytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return map_cuda(e);
+    if (perf) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        perf->time = ms * 1e-3;
+        perf->pairs = (double)steps * (double)n * ((double)p + (double)n - 1.0);
+        perf->performance = 0;
+        perf->wall_time = std::chrono::duration<double>(clock::now() - t_start).count();
+        perf->progress = 1.0;
+    }
+    return EM_OK;
+}
+
+} // namespace
+} // namespace em
+
+extern "C" {
+
+int em_verlet_step_f32(float *dyn, float *accel, size_t n, const float *charges, size_t p,
+                       const float *box_min, const float *box_max, float dt, size_t steps,
+                       const em_options *opt, em_perf *perf)
+{
+    return em::verlet<float>(dyn, accel, n, charges, p, box_min, box_max, dt, steps, opt, perf);
+}
+
+int em_verlet_step_f64(double *dyn, double *accel, size_t n, const double *charges, size_t p,
+                       const double *box_min, const double *box_max, double dt, size_t steps,
+                       const em_options *opt, em_perf *perf)
+{
+    return em::verlet<double>(dyn, accel, n, charges, p, box_min, box_max, dt, steps, opt,
+                              perf);
+}
+
+} // extern "C"

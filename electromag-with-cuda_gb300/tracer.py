@@ -383,6 +383,37 @@ def calc_field_multi(x, y, z, charges, n, devices, resolution=1.0,
     return rc, perf, ran.tolist(), int(nfailed.value)
 
 
+def verlet_step(dyn, accel, charges, box_min, box_max, dt, steps=1,
+                stream=None):
+    """Velocity-Verlet steps of moving charges (em_verlet_step_*), in place.
+    dyn (n, 8) {x, y, z, q, vx, vy, vz, m}, accel (n, 3), charges (p, 4):
+    numpy arrays, or CUDA tensors (then on the current torch stream).
+    Returns the perf record."""
+    lib = _capi.load()
+    dev = _is_torch(dyn) and dyn.is_cuda
+    f32 = str(dyn.dtype).endswith("float32")
+    for a in (dyn, accel, charges):
+        _check(a, "float32" if f32 else "float64")
+    n = dyn.shape[0]
+    p = charges.shape[0]
+    npt = np.float32 if f32 else np.float64
+    lo = np.ascontiguousarray(box_min, npt)
+    hi = np.ascontiguousarray(box_max, npt)
+    o = _capi.EmOptions()
+    if dev:
+        import torch
+        o.device_ptrs = 1
+        o.stream = (stream if stream is not None else
+                    torch.cuda.current_stream(dyn.device).cuda_stream)
+    perf = _capi.EmPerf()
+    fn = lib.em_verlet_step_f32 if f32 else lib.em_verlet_step_f64
+    rc = fn(_ptr(dyn), _ptr(accel), n, _ptr(charges), p, lo.ctypes.data,
+            hi.ctypes.data, dt, steps, ctypes_byref(o), ctypes_byref(perf))
+    if rc:
+        raise _capi.EmError(rc, "em_verlet_step")
+    return perf
+
+
 def trace_batch(sets, max_steps, resolution=1.0, term_radius=0.5, *,
                 steps_per_line=None, store_rows=0, threads_per_line=0,
                 lines_per_item=0, first_budget=0, phases=0, tile_charges=0,

@@ -324,6 +324,28 @@ EM_API int em_calc_field_multi_f64(const int *devices, size_t ndevices,
                                    int use_curvature, const em_options *opt,
                                    em_perf *perf, size_t *nfailed, int *ran_on);
 
+/* One or more velocity-Verlet steps of moving point charges (emgVerletStep,
+ * ElectroMag/src/Particle_System.cpp:109-190; no counterpart runs in the
+ * reference, whose template is never instantiated).  dyn: n records
+ * {x, y, z, q, vx, vy, vz, m} (dynamicPointCharge, Electrodynamics.h:29-34),
+ * updated in place; accel: n x 3, a(t) in and a(t + dt) out.  Per step and
+ * particle, from the start-of-step states of the others: v' = v + a dt/2,
+ * r' = r + v' dt; E = K sum over the static charges (p records {x,y,z,q})
+ * and the other particles of q r / |r|^3 at r'; B = 1e-7 sum over the other
+ * particles of q v x r / |r|^3; a = q (E + v' x B) / m; v = v' + a dt/2;
+ * then reflection off the walls of [box_min, box_max].  Returns 1 for n == 0
+ * (the reference's check).  Host pointers unless opt->device_ptrs. */
+EM_API int em_verlet_step_f32(float *dyn, float *accel, size_t n,
+                              const float *charges, size_t p,
+                              const float *box_min, const float *box_max,
+                              float dt, size_t steps, const em_options *opt,
+                              em_perf *perf);
+EM_API int em_verlet_step_f64(double *dyn, double *accel, size_t n,
+                              const double *charges, size_t p,
+                              const double *box_min, const double *box_max,
+                              double dt, size_t steps, const em_options *opt,
+                              em_perf *perf);
+
 /* ---- the reference program's inputs and outputs (host code) --------------
  * Presets of ElectroMag.cpp:43-55 (SimulationParams: lines nx*ny*nz, static
  * charges, rows per line), selected there by --bogo, --micro, --enhanced,
