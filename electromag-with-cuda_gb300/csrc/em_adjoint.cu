@@ -58,11 +58,12 @@ __device__ __forceinline__ float lane_sum(float v)
     return v;
 }
 
-// Loss sum (v - t)^2 over all vertices, FP64 partials, one atomic per CTA.
+// Loss sum (v - t)^2 over all vertices: one FP64 partial per CTA (part),
+// summed in CTA order by adj_loss_sum_kernel, so the loss repeats bit for bit.
 __global__ void __launch_bounds__(256) adj_loss_kernel(const float *x, const float *y,
                                                        const float *z, const float *tx,
                                                        const float *ty, const float *tz,
-                                                       size_t elems, double *loss)
+                                                       size_t elems, double *part)
 {
     double acc = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < elems;
@@ -73,15 +74,25 @@ __global__ void __launch_bounds__(256) adj_loss_kernel(const float *x, const flo
     }
     for (int o = 16; o; o >>= 1)
         acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    __shared__ double part[8];
+    __shared__ double wpart[8];
     if ((threadIdx.x & 31) == 0)
-        part[threadIdx.x >> 5] = acc;
+        wpart[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-            s += part[w];
-        atomicAdd(loss, s);
+            s += wpart[w];
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void adj_loss_sum_kernel(const double *part, int n, double *loss)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0;
+        for (int i = 0; i < n; ++i)
+            s += part[i];
+        *loss = s;
     }
 }
 
@@ -594,6 +605,8 @@ __global__ void adj_finish_kernel(const AdjParams P, double *grad)
 
 } // namespace
 
+int adjoint_loss_parts(int nsm) { return nsm * 4; }
+
 int adjoint_charge_blocks(int p)
 {
     return (p + kChargeThreads * kChargesPerThread - 1) / (kChargeThreads * kChargesPerThread);
@@ -684,9 +697,12 @@ cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, i
     if (e != cudaSuccess)
         return e;
     const size_t elems = (size_t)P.n * (size_t)P.rows;
-    adj_loss_kernel<<<nsm * 4, 256, 0, stream>>>(P.x, P.y, P.z, P.tx, P.ty, P.tz, elems, loss);
+    // loss[1 .. adjoint_loss_parts(nsm)] hold the per-CTA partials
+    adj_loss_kernel<<<nsm * 4, 256, 0, stream>>>(P.x, P.y, P.z, P.tx, P.ty, P.tz, elems,
+                                                 loss + 1);
+    adj_loss_sum_kernel<<<1, 32, 0, stream>>>(loss + 1, nsm * 4, loss);
     adj_init_kernel<<<(unsigned)((P.n + 255) / 256), 256, 0, stream>>>(P);
-    count_launch(2);
+    count_launch(3);
     const int seg = P.seg;
     if (fused) {
         if (P.stored) {

@@ -81,7 +81,7 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     // adjoint workspace: abar (3n f32); records (6 * seg * n f32, two-pass)
     // or the field (3 * rows * n f32 stored, 3 * seg * n f32 recomputed) and
     // the team partials (teams * 4 * p_bwd float2, fused); slice partials
-    // (slices * p * 4 f64); loss + grad (1 + 4p f64)
+    // (slices * p * 4 f64); the loss and its per-CTA partials, then grad (4p f64)
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t field_rows = stored ? rows : (size_t)kSeg;
     const size_t off_rec = up(3 * n * 4);
@@ -90,7 +90,7 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     const size_t tpart_bytes = fused ? (size_t)af.teams * 4 * (size_t)af.p_bwd * 8 : 0;
     const size_t off_part = off_tpart + up(tpart_bytes);
     const size_t off_loss = off_part + up((size_t)slices * p * 4 * 8);
-    const size_t off_grad = off_loss + 256;
+    const size_t off_grad = off_loss + up(8 * (1 + (size_t)adjoint_loss_parts(c.nsm)));
     const size_t need = off_grad + 4 * p * 8;
     if ((code = grow(&c.adj, &c.adj_cap, need)))
         return code;

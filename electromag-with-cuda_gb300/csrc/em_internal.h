@@ -135,6 +135,8 @@ struct AdjFused {
     size_t smem;
 };
 int adjoint_charge_blocks(int p);
+// FP64 slots after the loss that hold its per-CTA partials
+int adjoint_loss_parts(int nsm);
 // Fills *f and returns 1 when the fused backward applies to p charges.
 int adjoint_fused_plan(int p, int nsm, AdjFused *f);
 // fused == nullptr: the two-pass backward (field recompute + Jacobian-vector
