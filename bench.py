@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the extended / precision / adjoint blocks")
     ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint",
-                                       "adjoint-checkpoint"],
+                                       "adjoint-checkpoint", "batch"],
                     default=None,
                     help="profiling cases: run one small case and exit")
     return ap.parse_args()
@@ -204,12 +204,27 @@ def run_reference(args):
 
 def run_case(args):
     """Small profiling cases (ncu captures): the extended kernel on the
-    4096-charge workload (200 rows, no termination radius), or the adjoint
+    4096-charge workload (200 rows, no termination radius), the adjoint
     kernels on the 1024-charge workload (200 rows; stored field, or the
-    field recomputed per 64-row segment)."""
+    field recomputed per 64-row segment), or the batched tracer on the first
+    24 sets of the 512-set workload with the bench's tuned shape (limits
+    capped at 500 rows)."""
     import torch
     em = importlib.import_module("electromag-with-cuda_gb300")
     dev = torch.device("cuda", 0)
+    if args.case == "batch":
+        sets = em.workloads.make_batch(512, args.seed)[:24]
+        lims = np.concatenate([np.full(len(s), min(lim, 500), np.int32)
+                               for _, s, lim in sets])
+        kw = dict(threads_per_line=16, lines_per_item=256, first_budget=512,
+                  tile_charges=1024, stages=2)
+        for _ in range(2):
+            out = em.trace_batch([(c, s) for c, s, _ in sets], 500, 1.0, 0.5,
+                                 steps_per_line=lims, **kw)
+        torch.cuda.synchronize()
+        perf = out["perf"]
+        print("batch", perf.pairs / perf.time / 1e9, "Gpair/s")
+        return 0
     if args.case.startswith("ext"):
         ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)
         ch = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).to(dev)
