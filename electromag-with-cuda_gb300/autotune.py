@@ -21,10 +21,10 @@ CACHE = os.environ.get("EM_AUTOTUNE_CACHE",
                                     "autotune_cache.json"))
 
 SPACE = {
-    "threads_per_line": [8, 4, 16],
+    "threads_per_line": [16, 8, 4],
     "lines_per_item": [512, 256, 1024],
-    "first_budget": [256, 128, 512],
-    "tile_charges": [1024, 512, 2048],
+    "first_budget": [64, 32, 128, 256, 512],
+    "tile_charges": [1024, 2048, 512],
     "stages": [4, 3, 2],
 }
 
@@ -64,12 +64,14 @@ def _time(sets, max_steps, lims, opts, repeats=2):
 
 
 def tune_batch(sets, max_steps, steps_per_line=None, sample=32, seed=0,
-               rounds=2, use_cache=True, lines_cap=1024, steps_cap=1000):
+               rounds=2, use_cache=True, lines_cap=1024, steps_cap=None):
     """Returns the best option dict for trace_batch on these sets.
 
     Trials run on `sample` sets drawn at random, each cut to its first
-    `lines_cap` lines and to at most `steps_cap` steps: the ranking of
-    shapes follows the same mix of set sizes at a fraction of the cost."""
+    `lines_cap` lines: the same mix of set sizes and the same step limits (a
+    few long lines carry most of the pairs, and the phase budgets are tuned
+    for them, so steps are not capped unless `steps_cap` is given) at a
+    fraction of the cost."""
     key = _device_key() + "|" + _signature(sets, max_steps)
     cache = _load() if use_cache else {}
     if key in cache:
@@ -77,14 +79,15 @@ def tune_batch(sets, max_steps, steps_per_line=None, sample=32, seed=0,
     rng = np.random.default_rng(seed)
     idx = np.sort(rng.choice(len(sets), min(sample, len(sets)), replace=False))
     sub = [(sets[i][0], sets[i][1][:lines_cap]) for i in idx]
+    cap = max_steps if steps_cap is None else steps_cap
     lims = None
     if steps_per_line is not None:
         offs = np.concatenate([[0], np.cumsum([len(s) for _, s in sets])])
         lims = np.concatenate([
             np.minimum(steps_per_line[offs[i]:offs[i] + min(lines_cap,
                                                            offs[i + 1] - offs[i])],
-                       steps_cap) for i in idx]).astype(np.int32)
-    max_steps = min(max_steps, steps_cap)
+                       cap) for i in idx]).astype(np.int32)
+    max_steps = min(max_steps, cap)
     best = {k: v[0] for k, v in SPACE.items()}
     best_t = _time(sub, max_steps, lims, best)
     trials = [(dict(best), best_t)]

@@ -55,11 +55,14 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
     em_batch_options o{};
     if (opt)
         o = *opt;
-    const int tpl = o.threads_per_line ? o.threads_per_line : 8;
+    const int tpl = o.threads_per_line ? o.threads_per_line : 16;
     if (tpl != 4 && tpl != 8 && tpl != 16)
         return EM_ERR_ARG;
     const int item_lines = o.lines_per_item > 0 ? o.lines_per_item : 512;
-    const int first_budget = o.first_budget > 0 ? o.first_budget : 256;
+    // most lines of a set end within a few dozen steps while the few that
+    // run to their limit carry most of the pairs: a short first phase hands
+    // those on, grouped by set, before they can hold a CTA alone
+    const int first_budget = o.first_budget > 0 ? o.first_budget : 64;
     const int phases = o.phases > 0 ? std::min(o.phases, 8) : 4;
     const int stages = o.stages > 0 ? std::min(o.stages, 8) : 4;
     if (o.device_ptrs && ((uintptr_t)charges & 15))
@@ -120,7 +123,17 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
     for (size_t i = 0; i < order.size(); ++i)
         sorted_items[i] = items0[order[i]];
     const int nitems0 = (int)sorted_items.size();
-    const long long max_next_items = (long long)nsets + N / item_lines + 1;
+    // continuation items: the lines one CTA holds at once (31 compute warps,
+    // 32/tpl lines each); the lines still running after a phase are the long
+    // ones, of near-equal length within a set, so such an item keeps every
+    // warp busy to its end, and small items balance the CTAs
+    const int cont_lines = 31 * (32 / tpl);
+    const long long max_next_items = (long long)nsets + N / cont_lines + 1;
+    std::vector<int> set_order(nsets);
+    std::iota(set_order.begin(), set_order.end(), 0);
+    std::stable_sort(set_order.begin(), set_order.end(), [&](int a, int b) {
+        return charge_off[a + 1] - charge_off[a] > charge_off[b + 1] - charge_off[b];
+    });
 
     // ---- device workspace ------------------------------------------------------
     Buf B;
@@ -134,6 +147,7 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
     const size_t o_st = B.add((size_t)N * 16);
     const size_t o_cont = B.add((size_t)N * 8), o_conts = B.add((size_t)N * 8);
     const size_t o_setq = B.add(nsets * 4 * 3 + nsets * 8 + 64);
+    const size_t o_order = B.add(nsets * 4);
     size_t o_raw = 0, o_lines = 0, o_spl = 0, o_out = 0, o_rows = 0;
     const bool host = !o.device_ptrs;
     if (host) {
@@ -189,6 +203,7 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
     H2D(w + o_coff, coff.data(), (nsets + 1) * 8);
     H2D(w + o_loff, loff.data(), (nsets + 1) * 8);
     H2D(w + o_items0, sorted_items.data(), (size_t)nitems0 * 16);
+    H2D(w + o_order, set_order.data(), nsets * 4);
     if (host) {
         H2D((void *)d_charges, charges, (size_t)Pt * 16);
         H2D((void *)d_sx, sx, (size_t)N * 4);
@@ -263,6 +278,7 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
     Q.next_items = reinterpret_cast<int4 *>(w + o_itemsn);
     Q.next_nitems = nitemsn;
     Q.next_item_ctr = ctrn;
+    Q.set_order = reinterpret_cast<const int *>(w + o_order);
 
     const int threads = 1024; // 31 compute warps + 1 copy warp
     H2D(nitems0_d, &nitems0, 4);
@@ -292,7 +308,7 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
             r = launch_batch_trace(Pp, tpl, c.nsm, threads, smem, st);
             if (r == cudaSuccess && ph + 1 < phases)
                 r = launch_batch_sort(Q, reinterpret_cast<const long long *>(w + o_loff),
-                                      (int)nsets, item_lines, st);
+                                      (int)nsets, cont_lines, st);
             budget = budget > INT_MAX / 4 ? INT_MAX : budget * 4;
         }
         return r;

@@ -185,6 +185,7 @@ struct BatchQueues {
     int4 *next_items;
     int *next_nitems;
     unsigned *next_item_ctr;
+    const int *set_order;            // sets by descending charge count
 };
 cudaError_t launch_batch_stage(const float *raw, const long long *coff, const long long *soff,
                                const int *spad, int gran, int nsets, float *staged, int *snneg,

@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(256) batch_stage_kernel(const float *raw,
 }
 
 // ---- continuation list -> next phase's items (one CTA) ---------------------
-// counts per set, scan, scatter of line ids by set, then items of at most
-// item_lines lines per set.
+// counts per set, scan (largest set first), scatter of line ids by set, then
+// items of at most item_lines lines per set.
 __device__ __forceinline__ int set_of(const long long *line_off, int nsets, long long id)
 {
     int lo = 0, hi = nsets; // line_off[lo] <= id < line_off[hi]
@@ -119,11 +119,13 @@ __global__ void __launch_bounds__(1024) batch_sort_kernel(BatchQueues Q, const l
         atomicAdd(&Q.set_count[set_of(line_off, nsets, Q.cont[i])], 1);
     __syncthreads();
     if (tid == 0) {
-        // sequential scan over sets (few thousand at most): line offsets and
-        // item offsets
+        // sequential scan over sets (few thousand at most), largest set
+        // first: line offsets and item offsets, so the next phase deals the
+        // longest items first
         long long lo = 0;
         int it = 0;
-        for (int s = 0; s < nsets; ++s) {
+        for (int o = 0; o < nsets; ++o) {
+            const int s = Q.set_order[o];
             const int k = Q.set_count[s];
             Q.set_line_off[s] = lo;
             Q.set_item_off[s] = it;

@@ -231,9 +231,12 @@ EM_API int em_adjoint_f32(float *x, float *y, float *z, size_t n, size_t rows,
  * NULL when store_rows == 0).  Host pointers unless opt->device_ptrs.
  * perf->pairs counts field evaluations x the set's charge count. */
 typedef struct em_batch_options {
-    int threads_per_line; /* 0: 8; else 4, 8 or 16 (lanes per line)         */
-    int lines_per_item;   /* 0: 512 lines per work item                      */
-    int first_budget;     /* 0: 256 field evaluations per line in phase 0;
+    int threads_per_line; /* 0: 16; else 4, 8 or 16 (lanes per line)        */
+    int lines_per_item;   /* 0: 512 lines per phase-0 work item; later
+                             phases' items hold the lines of one set that a
+                             CTA traces at once (31 * 32 / threads_per_line),
+                             largest sets first                              */
+    int first_budget;     /* 0: 64 field evaluations per line in phase 0;
                              each later phase has four times more, the last
                              is unlimited                                    */
     int phases;           /* 0: 4                                            */

@@ -22,13 +22,19 @@ def make_sets(em, nsets, seed, pmin=16, pmax=400, per_pos=4):
     return sets
 
 
-def per_set(em, sets, max_steps, lims, store_rows):
+BATCH_DEFAULT_TPL = 16   # em_batch_options.threads_per_line = 0
+
+
+def per_set(em, sets, max_steps, lims, store_rows, tpl=BATCH_DEFAULT_TPL):
+    """Each set through em_trace_lines with the batch's lanes per line (the
+    same lane order, hence the same bits)."""
     out, k = [], 0
     for ch, seeds in sets:
         m = len(seeds)
         r = em.trace_lines(seeds, ch, max_steps, 1.0, 0.5,
                            steps_per_line=lims[k:k + m] if lims is not None
-                           else None, deterministic=True)
+                           else None, deterministic=True,
+                           threads_per_line=tpl)
         out.append(r)
         k += m
     return out
@@ -59,12 +65,15 @@ def batch_case(em):
 
 @pytest.mark.parametrize("kw", [dict(), dict(first_budget=8, phases=4),
                                 dict(use_graph=True),
-                                dict(lines_per_item=16, threads_per_line=8)])
+                                dict(lines_per_item=16, threads_per_line=8),
+                                dict(threads_per_line=4, first_budget=4,
+                                     phases=6)])
 def test_batch_equals_per_set_calls(em, gpu, batch_case, kw):
     sets, lims = batch_case
     b = em.trace_batch(sets, 300, 1.0, 0.5, steps_per_line=lims, store_rows=24,
                        deterministic=True, **kw)
-    ref = per_set(em, sets, 300, lims, 24)
+    ref = per_set(em, sets, 300, lims, 24,
+                  kw.get("threads_per_line", BATCH_DEFAULT_TPL))
     check_equal(b, ref, sets, 24)
     total = sum(float(np.sum(r["perf"].pairs)) for r in ref)
     assert b["perf"].pairs == total
