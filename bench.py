@@ -216,8 +216,8 @@ def run_case(args):
         sets = em.workloads.make_batch(512, args.seed)[:24]
         lims = np.concatenate([np.full(len(s), min(lim, 500), np.int32)
                                for _, s, lim in sets])
-        kw = dict(threads_per_line=16, lines_per_item=256, first_budget=512,
-                  tile_charges=1024, stages=2)
+        kw = dict(threads_per_line=16, lines_per_item=512, first_budget=64,
+                  tile_charges=2048, stages=4)
         for _ in range(2):
             out = em.trace_batch([(c, s) for c, s, _ in sets], 500, 1.0, 0.5,
                                  steps_per_line=lims, **kw)
