@@ -2,7 +2,8 @@
 
 Lines never interact, so the path shards by contiguous line ranges with no
 exchange during tracing; results are gathered only if the caller wants them
-in one place.  The reference's multi-device split
+in one place, and the adjoint's charge gradients are summed with one
+all-reduce.  The reference's multi-device split
 (GPGPU_Segment/src/CL_Electrostatics.cpp:113-183) sizes shares by compute
 units; here ranks are identical GPUs, so shares differ by at most one line.
 """
@@ -35,3 +36,26 @@ def gather_lines(local, n, world, rank, group=None):
         rb, re_ = shard_range(n, world, r)
         out.append(parts[r][: re_ - rb])
     return torch.cat(out).numpy()
+
+
+def adjoint_sharded(grad_fn, seeds, targets, world, rank, group=None):
+    """Loss and charge gradients over lines sharded across ranks.
+
+    The loss is a sum over lines and the gradient with respect to the
+    charges is a sum of per-line terms, so each rank runs the adjoint on its
+    contiguous range of lines and one all-reduce (sum) of the loss and the
+    4p gradient entries completes it — the only exchange of the path.
+    grad_fn(seeds_shard, targets_shard) -> (loss, grad (p, 4)) runs one
+    shard (em.adjoint on this rank's GPU); targets are (3, rows, n).
+    Returns (loss, grad) identical on every rank."""
+    import torch
+    import torch.distributed as dist
+    n = len(seeds)
+    b, e = shard_range(n, world, rank)
+    loss, grad = grad_fn(seeds[b:e], targets[:, :, b:e])
+    buf = torch.zeros(1 + np.asarray(grad).size, dtype=torch.float64)
+    buf[0] = float(loss)
+    buf[1:] = torch.as_tensor(np.asarray(grad, np.float64).ravel())
+    dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+    out = buf.numpy()
+    return float(out[0]), out[1:].reshape(np.shape(grad))

@@ -62,3 +62,56 @@ def test_two_gloo_ranks_equal_single_process(em, orc, tmp_path):
     _, ln, cl = orc.trace_lines_f64(ch.astype(np.float64), seeds, 30, 1.0, 0.5)
     assert np.array_equal(g["len"], ln)
     assert np.array_equal(g["cls"], cl)
+
+
+def _adjoint_worker(rank, world, port, out_path):
+    import sys
+    import torch.distributed as dist
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    sys.path.insert(0, os.path.join(root, "oracle"))
+    sys.path.insert(0, os.path.join(root, "tests"))
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import importlib
+    em = importlib.import_module("electromag-with-cuda_gb300")
+    import em_oracle as orc
+    ch, seeds, rows, targets = _adjoint_inputs()
+
+    def shard_grad(s, t):
+        # the FP64 discrete adjoint of this rank's lines (the GPU path calls
+        # em.adjoint here)
+        fz = orc.Frozen(ch, s, rows, t)
+        return fz.L, fz.grad()
+
+    L, g = em.shard.adjoint_sharded(shard_grad, seeds, targets, world, rank)
+    np.savez(out_path + f".{rank}.npz", loss=L, grad=g)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def _adjoint_inputs():
+    rng = np.random.default_rng(11)
+    p, n, rows = 16, 37, 12
+    ch = np.zeros((p, 4))
+    ch[:, :3] = rng.uniform(-10, 10, (p, 3))
+    ch[:, 3] = rng.uniform(1, 10, p) * rng.choice([-1, 1], p, p=[0.3, 0.7])
+    d = rng.normal(size=(n, 3))
+    seeds = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(35, 45, (n, 1))
+    targets = rng.normal(0, 40, (3, rows, n))
+    return ch, seeds, rows, targets
+
+
+def test_sharded_adjoint_equals_single_process(em, orc, tmp_path):
+    """Two gloo ranks, 18 and 19 lines: one all-reduce of loss and
+    gradients gives the one-process adjoint of all 37 lines on both ranks."""
+    out = str(tmp_path / "adj")
+    mp.spawn(_adjoint_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    ch, seeds, rows, targets = _adjoint_inputs()
+    fz = orc.Frozen(ch, seeds, rows, targets)
+    ref_g = fz.grad()
+    for r in range(2):
+        z = np.load(out + f".{r}.npz")
+        assert float(z["loss"]) == pytest.approx(fz.L, rel=1e-12)
+        assert np.allclose(z["grad"], ref_g, rtol=1e-10, atol=1e-12 * np.abs(ref_g).max())
