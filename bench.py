@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--pack", default="auto")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the extended / precision / adjoint blocks")
+                    help="skip the single-GPU blocks of the other workloads "
+                         "(always skipped when N > 1)")
     ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint",
                                        "adjoint-checkpoint", "batch"],
                     default=None,
@@ -323,7 +324,7 @@ def main():
         e2e = run_e2e(em, torch, dist, ch, seeds, rows, args, world)
 
     extras = {}
-    if not args.no_extras:
+    if not args.no_extras and world == 1:
         extras = run_extras(em, torch, dev, args)
 
     cpu = None
@@ -615,15 +616,24 @@ def reference_run_block(em, torch, dev, seed):
 
 
 def run_extras(em, torch, dev, args):
+    """Single-GPU measurements of the other configurations; a block that
+    fails is reported in its place and does not cost the bench line."""
+    blocks = [
+        ("reference_run", lambda: reference_run_block(em, torch, dev, args.seed)),
+        ("batched", lambda: batch_block(em, torch, dev, args.seed)),
+        ("precision", lambda: precision_block(em, torch, dev, args.workload,
+                                              5000, args.seed, 20000, True)),
+        ("precision_stress", lambda: precision_block(
+            em, torch, dev, "dipole_16384", 4000, args.seed, 20000, False)),
+        ("adjoint", lambda: adjoint_block(em, torch, dev, args.seed)),
+    ]
     out = {}
-    out["reference_run"] = reference_run_block(em, torch, dev, args.seed)
-    out["batched"] = batch_block(em, torch, dev, args.seed)
-    out["precision"] = precision_block(em, torch, dev, args.workload, 5000,
-                                       args.seed, 20000, True)
-    out["precision_stress"] = precision_block(em, torch, dev, "dipole_16384",
-                                              4000, args.seed, 20000, False)
-    out["adjoint"] = adjoint_block(em, torch, dev, args.seed)
-    torch.cuda.empty_cache()
+    for name, fn in blocks:
+        try:
+            out[name] = fn()
+        except Exception as exc:  # reported, not fatal
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
     return out
 
 
