@@ -87,7 +87,10 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
         for (int j = t; j < count; j += TPL)
             pair_fast<T>(px, py, pz, load_charge(tile, j), a.x, a.y, a.z);
     } else {
-#pragma unroll 2
+        // one lane per line (the reference's charge order): the rounded
+        // divides and roots of consecutive charges are independent, only the
+        // sums are ordered, so a deep unroll keeps several pairs in flight
+#pragma unroll(sizeof(T) == 4 ? 8 : 2)
         for (int j = t; j < count; j += TPL)
             pair_exact<T>(px, py, pz, load_charge(tile, j), K, three_arg, a.x, a.y, a.z);
     }
