@@ -40,7 +40,9 @@ DevCtx *get_ctx(int *code)
         c.nsm = prop.multiProcessorCount;
         c.smem_optin = prop.sharedMemPerBlockOptin;
         if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreate(&c.ev0) != cudaSuccess || cudaEventCreate(&c.ev1) != cudaSuccess) {
+            cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&c.ev0) != cudaSuccess || cudaEventCreate(&c.ev1) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c.ev_chunk, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
             *code = EM_ERR_CUDA;
             return nullptr;
@@ -214,14 +216,53 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     prm.resolution = resolution;
     prm.err = c.err;
 
+    // Host arrays, all lines: trace in row chunks and copy each finished
+    // chunk to the host on the copy stream while the next one is traced
+    // (rows are contiguous blocks of n values; a chunk resumes from the last
+    // row of the one before, so the result is the one-launch result).
+    const bool chunked = !o.device_ptrs && nl == n && elems * sizeof(T) * 3 >= (64u << 20) &&
+                         total_steps >= 64;
+    const int nchunks = chunked ? 8 : 1;
     e = cudaEventRecord(c.ev0, s);
-    if (e == cudaSuccess)
-        e = launch_ref_trace<T>(prm, pl.cfg, pl.arith, s);
+    for (int k = 0; k < nchunks && e == cudaSuccess; ++k) {
+        const int r0 = 1 + (int)(((long long)(total_steps - 1) * k) / nchunks);
+        const int r1 = 1 + (int)(((long long)(total_steps - 1) * (k + 1)) / nchunks);
+        // rows [r0, r1) from row r0 - 1: the arrays seen from row r0 - 1
+        RefTraceParams<T> q = prm;
+        const size_t base = (size_t)(r0 - 1) * n;
+        q.x = dx + base;
+        q.y = dy + base;
+        q.z = dz + base;
+        q.seed_x = dx;
+        q.seed_y = dy;
+        q.seed_z = dz;
+        q.total_steps = r1 - r0 + 1;
+        e = launch_ref_trace<T>(q, pl.cfg, pl.arith, s);
+        if (e == cudaSuccess && chunked) {
+            e = cudaEventRecord(c.ev_chunk, s);
+            if (e == cudaSuccess)
+                e = cudaStreamWaitEvent(c.copy_stream, c.ev_chunk, 0);
+            const size_t off = (size_t)r0 * n, cnt = (size_t)(r1 - r0) * n;
+            T *dst[3] = {x, y, z};
+            const T *src[3] = {dx, dy, dz};
+            for (int d = 0; d < 3 && e == cudaSuccess; ++d)
+                e = cudaMemcpyAsync(dst[d] + off, src[d] + off, cnt * sizeof(T),
+                                    cudaMemcpyDeviceToHost, c.copy_stream);
+        }
+    }
     if (e == cudaSuccess)
         e = cudaEventRecord(c.ev1, s);
+    if (e == cudaSuccess && chunked) {
+        // the call's stream waits for the last copies, so it completes as one
+        e = cudaEventRecord(c.ev_chunk, c.copy_stream);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(s, c.ev_chunk, 0);
+    }
     if (e != cudaSuccess)
         return map_cuda(e);
-    if (!o.device_ptrs && nl == n) {
+    if (chunked) {
+        // copies already enqueued
+    } else if (!o.device_ptrs && nl == n) {
         const size_t rest = elems - n;
         e = cudaMemcpyAsync(x + n, dx + n, rest * sizeof(T), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess)

@@ -46,7 +46,7 @@ template <class T> struct RefTraceParams {
     const void *charges;       // padded charge records, 16-B aligned
     long long n;               // number of lines (row stride)
     long long n_groups;        // ceil(n / lines_per_warp)
-    int total_steps;           // rows, including the seed row
+    int total_steps;           // rows, including the start row
     int p_pad;                 // padded charge count (resident: all; streamed: n_tiles*tile)
     int n_tiles;               // streamed: number of charge tiles
     int tile_recs;             // streamed: records per tile
@@ -58,6 +58,9 @@ template <class T> struct RefTraceParams {
     // optional: the charge sum E/K (fast arithmetic) at vertex s of each
     // line, stored at (s * n + line) for s < total_steps - 1 (null: none)
     T *fx, *fy, *fz;
+    // the seeds the SSE rule's curvature reads (null: row 0 of x, y, z); a
+    // launch that resumes a trace passes x, y, z from its start row
+    const T *seed_x, *seed_y, *seed_z;
 };
 
 // Extended tracer (em_trace_ext.cu).

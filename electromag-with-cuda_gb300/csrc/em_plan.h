@@ -21,7 +21,8 @@ struct DevCtx {
     int nsm = 0;
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t copy_stream = nullptr; // device-to-host copies overlapped with tracing
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_chunk = nullptr;
     void *charges = nullptr; // staged (padded, possibly paired) charges
     size_t charges_cap = 0;
     void *charges_raw = nullptr; // the caller's records, copied as given

@@ -303,9 +303,9 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                 // (CPU_Implement.cpp:148-153)
                 T r0x = px[k], r0y = py[k], r0z = pz[k];
                 if (P.rule == RULE_SSE && own[k]) {
-                    r0x = ld_seed(P.x + line[k]);
-                    r0y = ld_seed(P.y + line[k]);
-                    r0z = ld_seed(P.z + line[k]);
+                    r0x = ld_seed(P.seed_x + line[k]);
+                    r0y = ld_seed(P.seed_y + line[k]);
+                    r0z = ld_seed(P.seed_z + line[k]);
                 }
                 advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k], py[k],
                            pz[k]);
@@ -394,9 +394,15 @@ cudaError_t launch_packed(const RefTraceParams<T> &p, const LaunchCfg &cfg, cuda
 } // namespace
 
 template <class T>
-cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
+cudaError_t launch_ref_trace(const RefTraceParams<T> &params, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream)
 {
+    RefTraceParams<T> p = params;
+    if (!p.seed_x) {
+        p.seed_x = p.x;
+        p.seed_y = p.y;
+        p.seed_z = p.z;
+    }
     if (cfg.kl != 1 && (cfg.kl != 2 || arith == ARITH_EXACT))
         return cudaErrorInvalidValue;
     if (arith == ARITH_EXACT) {

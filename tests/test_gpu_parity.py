@@ -246,3 +246,25 @@ def test_field_f64_matches_fp64_oracle(em, gpu, orc, cpu_config):
     e_gpu = em.field(pts, ch.astype(np.float64), arith="exact")
     rel = np.linalg.norm(e_gpu - e_cpu, axis=1) / np.linalg.norm(e_cpu, axis=1)
     assert rel.max() <= 1e-13, rel.max()
+
+
+def test_host_entry_chunked_copy_matches_device_entry(em, gpu):
+    """Host arrays above 64 MB are traced in row chunks whose device-to-host
+    copies overlap the next chunk: the vertices equal the device-pointer
+    entry's (one launch) bit for bit."""
+    torch = pytest.importorskip("torch")
+    ch, seeds, _ = em.workloads.make("cpu_256", seed=5)
+    ch = np.ascontiguousarray(ch, np.float32)
+    seeds = np.tile(seeds.astype(np.float32), (8, 1))[:8192]
+    n, rows = len(seeds), 1000
+    x, y, z = lines_from(seeds, rows, np.float32)
+    rc, _ = em.calc_field(x, y, z, ch, n, 1.0, True, require_n64=False,
+                          plain=False)
+    assert rc == 0
+    D = [torch.from_numpy(lines_from(seeds, rows, np.float32)[c]).cuda()
+         for c in range(3)]
+    rc, _ = em.calc_field(*D, torch.from_numpy(ch).cuda(), n, 1.0, True)
+    torch.cuda.synchronize()
+    assert rc == 0
+    for host, dev in zip((x, y, z), D):
+        assert np.array_equal(host, dev.cpu().numpy())
