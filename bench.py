@@ -615,6 +615,62 @@ def reference_run_block(em, torch, dev, seed):
     return blk
 
 
+def nbody_functor_block(em, torch, dev, seed):
+    """The Verlet step of moving charges (65 536 particles in the field of
+    4096 static charges, 4 steps, FP32 and FP64) and the functor layer's
+    cost on one GPU (the 4096-charge workload's first 8192 lines x 1000 rows
+    through 4 line ranges on device 0, against one host-pointer call)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n, p, steps = 65536, 4096, 4
+    dyn = np.zeros((n, 8))
+    dyn[:, :3] = rng.uniform(-100, 100, (n, 3))
+    dyn[:, 3] = rng.uniform(-1, 1, n) * 1e-9
+    dyn[:, 4:7] = rng.normal(0, 1e3, (n, 3))
+    dyn[:, 7] = rng.uniform(1e-6, 1e-5, n)
+    st = np.zeros((p, 4))
+    st[:, :3] = rng.uniform(-100, 100, (p, 3))
+    st[:, 3] = rng.uniform(-1, 1, p) * 1e-8
+    box = ([-100.0] * 3, [100.0] * 3)
+    blk = {"workload": f"{n} moving + {p} static charges, {steps} steps"}
+    for name, dt in (("fp32", torch.float32), ("fp64", torch.float64)):
+        d = torch.from_numpy(dyn).to(dev, dt)
+        a = torch.zeros((n, 3), dtype=dt, device=dev)
+        c = torch.from_numpy(st).to(dev, dt)
+        em.verlet_step(d, a, c, *box, 1e-6, steps=1)  # warm-up
+        perf = em.verlet_step(d, a, c, *box, 1e-6, steps=steps)
+        torch.cuda.synchronize()
+        blk[name] = {"ms": perf.time * 1e3,
+                     "gpair_s": perf.pairs / perf.time / 1e9}
+    ch, seeds, _ = em.workloads.make("gpu_4096", seed=seed)
+    ch = np.ascontiguousarray(ch, np.float32)
+    seeds = seeds.astype(np.float32)[:8192]
+    nl, rows = len(seeds), 1000
+
+    def fresh():
+        x = np.zeros((3, rows * nl), np.float32)
+        x[:, :nl] = seeds.T
+        return x
+
+    x = fresh()
+    em.calc_field(x[0], x[1], x[2], ch, nl, 1.0, True, require_n64=False,
+                  plain=False)
+    t = time.perf_counter()
+    x = fresh()
+    rc, _ = em.calc_field(x[0], x[1], x[2], ch, nl, 1.0, True,
+                          require_n64=False, plain=False)
+    one = time.perf_counter() - t
+    y = fresh()
+    t = time.perf_counter()
+    rc2, _, ran, nfailed = em.calc_field_multi(y[0], y[1], y[2], ch, nl,
+                                               [0, 0, 0, 0])
+    multi = time.perf_counter() - t
+    blk["functor"] = {"one_call_s": one, "four_ranges_s": multi,
+                      "ranges_ran_on": ran, "failed": nfailed,
+                      "identical": bool(rc == 0 and rc2 == 0
+                                        and np.array_equal(x, y))}
+    return blk
+
+
 def run_extras(em, torch, dev, args):
     """Single-GPU measurements of the other configurations; a block that
     fails is reported in its place and does not cost the bench line."""
@@ -626,6 +682,7 @@ def run_extras(em, torch, dev, args):
         ("precision_stress", lambda: precision_block(
             em, torch, dev, "dipole_16384", 4000, args.seed, 20000, False)),
         ("adjoint", lambda: adjoint_block(em, torch, dev, args.seed)),
+        ("nbody_functor", lambda: nbody_functor_block(em, torch, dev, args.seed)),
     ]
     out = {}
     for name, fn in blocks:
