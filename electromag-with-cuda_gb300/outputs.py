@@ -43,6 +43,11 @@ def autoregress(cpu, gpu, threshold=0.1, path=None, stream=None):
     is_dev = hasattr(cpu, "is_cuda") and cpu.is_cuda
     if is_dev:
         import torch
+        for t in (cpu, gpu):
+            if t.dtype != torch.float32 or t.dim() != 3 or t.shape[0] != 3:
+                raise TypeError("autoregress takes (3, rows, n) float32 arrays")
+        if tuple(cpu.shape) != tuple(gpu.shape) or not gpu.is_cuda:
+            raise ValueError("both runs must be CUDA tensors of one shape")
         rows, n = cpu.shape[1], cpu.shape[2]
         a, b = cpu.contiguous(), gpu.contiguous()
         ptrs = [a[c].data_ptr() for c in range(3)] + [b[c].data_ptr() for c in range(3)]
@@ -51,6 +56,8 @@ def autoregress(cpu, gpu, threshold=0.1, path=None, stream=None):
                     torch.cuda.current_stream(a.device).cuda_stream)
         keep = (a, b)
     else:
+        if np.shape(cpu) != np.shape(gpu) or len(np.shape(cpu)) != 3:
+            raise ValueError("autoregress takes two (3, rows, n) arrays of one shape")
         rows, n = np.shape(cpu)[1], np.shape(cpu)[2]
         ha, pa = _host3(cpu, rows, n)
         hb, pb = _host3(gpu, rows, n)

@@ -132,3 +132,9 @@ def test_save_dump_reports_unwritable_path(em, tmp_path):
     with pytest.raises(em.EmError) as e:
         em.outputs.save_lines(tmp_path / "no" / "such" / "dir.txt", 2, 2, a)
     assert e.value.code == 15
+
+
+def test_autoregress_rejects_mismatched_runs(em):
+    a = np.zeros((3, 4, 5), np.float32)
+    with pytest.raises(ValueError):
+        em.outputs.autoregress(a, np.zeros((3, 4, 6), np.float32))
