@@ -146,7 +146,9 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     r.cfg.grid = (int)std::min<long long>(c.nsm, r.n_groups);
     r.cfg.resident = resident ? 1 : 0;
     if (resident) {
-        r.p_pad = (int)((p + gran - 1) / gran * gran);
+        // at least one granule of pad records: a call without charges traces
+        // a zero field (the reference then steps by 0/0 into NaN, code 0)
+        r.p_pad = (int)((std::max<size_t>(p, 1) + gran - 1) / gran * gran);
         r.n_tiles = 1;
         r.cfg.stages = 1;
         r.cfg.tile_recs = r.p_pad;

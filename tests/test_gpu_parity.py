@@ -268,3 +268,17 @@ def test_host_entry_chunked_copy_matches_device_entry(em, gpu):
     assert rc == 0
     for host, dev in zip((x, y, z), D):
         assert np.array_equal(host, dev.cpu().numpy())
+
+
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_no_charges_traces_a_zero_field(em, gpu, arith):
+    """Zero charges: the field is zero and the reference's step is 0/0, so
+    every row after the seeds is NaN and the call still returns 0."""
+    seeds = np.random.default_rng(2).uniform(-5, 5, (64, 3)).astype(np.float32)
+    x, y, z = lines_from(seeds, 6, np.float32)
+    rc, _ = em.calc_field(x, y, z, np.zeros((0, 4), np.float32), 64, 1.0,
+                          True, arith=arith, plain=False)
+    assert rc == 0
+    v = np.stack([x, y, z]).reshape(3, 6, 64)
+    assert np.array_equal(v[:, 0], seeds.T)
+    assert np.all(np.isnan(v[:, 1:]))
