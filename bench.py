@@ -56,7 +56,8 @@ def parse():
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
     ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint",
-                                       "adjoint-checkpoint", "batch"],
+                                       "adjoint-checkpoint", "adjoint-twopass",
+                                       "batch", "verlet"],
                     default=None,
                     help="profiling cases: run one small case and exit")
     return ap.parse_args()
@@ -207,9 +208,11 @@ def run_case(args):
     """Small profiling cases (ncu captures): the extended kernel on the
     4096-charge workload (200 rows, no termination radius), the adjoint
     kernels on the 1024-charge workload (200 rows; stored field, or the
-    field recomputed per 64-row segment), or the batched tracer on the first
-    24 sets of the 512-set workload with the bench's tuned shape (limits
-    capped at 500 rows)."""
+    field recomputed per 64-row segment; adjoint-twopass: 6000 charges, the
+    two-pass backward of sets above 4096 charges), the batched tracer on the
+    first 24 sets of the 512-set workload with the bench's tuned shape
+    (limits capped at 500 rows), or the Verlet step (65 536 moving and 4096
+    static charges, FP32, 2 steps)."""
     import torch
     em = importlib.import_module("electromag-with-cuda_gb300")
     dev = torch.device("cuda", 0)
@@ -236,7 +239,29 @@ def run_case(args):
         torch.cuda.synchronize()
         print(prec, out["perf"].pairs / out["perf"].time / 1e9, "Gpair/s")
         return 0
+    if args.case == "verlet":
+        rng = np.random.Generator(np.random.PCG64(args.seed))
+        n, p = 65536, 4096
+        dyn = np.zeros((n, 8), np.float32)
+        dyn[:, :3] = rng.uniform(-100, 100, (n, 3))
+        dyn[:, 3] = rng.uniform(-1, 1, n) * 1e-9
+        dyn[:, 4:7] = rng.normal(0, 1e3, (n, 3))
+        dyn[:, 7] = rng.uniform(1e-6, 1e-5, n)
+        st = np.zeros((p, 4), np.float32)
+        st[:, :3] = rng.uniform(-100, 100, (p, 3))
+        st[:, 3] = rng.uniform(-1, 1, p) * 1e-8
+        d = torch.from_numpy(dyn).to(dev)
+        a = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+        c = torch.from_numpy(st).to(dev)
+        for _ in range(2):
+            perf = em.verlet_step(d, a, c, [-100.0] * 3, [100.0] * 3, 1e-6,
+                                  steps=2)
+        torch.cuda.synchronize()
+        print("verlet", perf.pairs / perf.time / 1e9, "Gpair/s")
+        return 0
     ch_np, seeds_np, _ = em.workloads.make("adjoint_1024", seed=args.seed)
+    if args.case == "adjoint-twopass":
+        ch_np = em.workloads.uniform_charges(6000, 50.0, args.seed)
     rows, n = 200, len(seeds_np)
     ch = torch.from_numpy(np.ascontiguousarray(ch_np, np.float32)).to(dev)
     V = torch.zeros((3, rows, n), dtype=torch.float32, device=dev)

@@ -13,10 +13,11 @@
 //
 // Every particle sees the others' start-of-step states, exactly as the
 // reference's loop does (it reads dynCharges[j], which it never updates), so
-// particles are independent: one thread per particle, charges and particles
-// staged through shared memory in tiles (the all-pairs pattern of the field
-// tracer).  The tile that holds a thread's own particle runs the loop that
-// skips j = i; every other tile runs without the test.
+// particles are independent: 1, 2 or 4 lanes per particle (enough to fill
+// the SMs), charges and particles staged through shared memory in tiles (the
+// all-pairs pattern of the field tracer).  The tile that holds a block's
+// particles runs the loop that skips j = i; every other tile runs without
+// the test.
 #include <chrono>
 #include <climits>
 #include <cstdint>
@@ -36,6 +37,9 @@ constexpr int kVerletBlock = 128;
 
 template <class T> struct alignas(sizeof(T) * 4) Dyn {
     T x, y, z, q, vx, vy, vz, m; // dynamicPointCharge<T> (Electrodynamics.h:29-34)
+};
+template <class T> struct alignas(sizeof(T) * 4) Q4 {
+    T x, y, z, q; // pointCharge<T>
 };
 
 template <class T> __device__ __forceinline__ T inv_len3(T r2);
@@ -61,12 +65,12 @@ template <class T> struct VerletArgs {
     T dt;
 };
 
-template <class T, bool SELF>
-__device__ __forceinline__ void dyn_tile(const Dyn<T> *tile, int count, int self, T rx, T ry,
-                                         T rz, T &ex, T &ey, T &ez, T &bx, T &by, T &bz)
+template <class T, int TPP, bool SELF>
+__device__ __forceinline__ void dyn_tile(const Dyn<T> *tile, int count, int self, int t, T rx,
+                                         T ry, T rz, T &ex, T &ey, T &ez, T &bx, T &by, T &bz)
 {
 #pragma unroll 4
-    for (int j = 0; j < count; ++j) {
+    for (int j = t; j < count; j += TPP) {
         if (SELF && j == self)
             continue;
         const Dyn<T> d = tile[j];
@@ -86,12 +90,27 @@ __device__ __forceinline__ void dyn_tile(const Dyn<T> *tile, int count, int self
     }
 }
 
-template <class T>
+template <int TPP, class T> __device__ __forceinline__ T lanes_sum(T v)
+{
+#pragma unroll
+    for (int o = TPP / 2; o >= 1; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// TPP lanes share a particle and split its sums (j = t, t + TPP, ...), so a
+// modest particle count still fills the SMs; a block holds kVerletBlock/TPP
+// particles, all in one 128-record particle tile.
+template <class T, int TPP>
 __global__ void __launch_bounds__(kVerletBlock) verlet_kernel(const VerletArgs<T> A)
 {
     __shared__ Dyn<T> dtile[kVerletBlock];
-    __shared__ T stile[kVerletBlock * 4];
-    const long long i = blockIdx.x * (long long)kVerletBlock + threadIdx.x;
+    __shared__ Q4<T> stile_q[kVerletBlock];
+    T *stile = &stile_q[0].x;
+    constexpr int PPB = kVerletBlock / TPP; // particles per block
+    const int t = threadIdx.x % TPP;
+    const int local = threadIdx.x / TPP;
+    const long long i = blockIdx.x * (long long)PPB + local;
     const bool own = i < A.n;
     Dyn<T> me{};
     T ax = 0, ay = 0, az = 0;
@@ -110,32 +129,40 @@ __global__ void __launch_bounds__(kVerletBlock) verlet_kernel(const VerletArgs<T
     for (int t0 = 0; t0 < A.p; t0 += kVerletBlock) {
         const int cnt = min(kVerletBlock, A.p - t0);
         __syncthreads();
-        for (int k = threadIdx.x; k < cnt * 4; k += kVerletBlock)
-            stile[k] = A.charges[4 * (size_t)t0 + k];
+        for (int k = threadIdx.x; k < cnt; k += kVerletBlock)
+            reinterpret_cast<Q4<T> *>(stile)[k] = reinterpret_cast<const Q4<T> *>(A.charges)[t0 + k];
         __syncthreads();
 #pragma unroll 4
-        for (int j = 0; j < cnt; ++j) {
-            const T dx = rx - stile[4 * j], dy = ry - stile[4 * j + 1],
-                    dz = rz - stile[4 * j + 2];
+        for (int j = t; j < cnt; j += TPP) {
+            const Q4<T> c = reinterpret_cast<const Q4<T> *>(stile)[j];
+            const T dx = rx - c.x, dy = ry - c.y, dz = rz - c.z;
             const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-            const T w = stile[4 * j + 3] * inv_len3<T>(r2);
+            const T w = c.q * inv_len3<T>(r2);
             ex = fma(w, dx, ex);
             ey = fma(w, dy, ey);
             ez = fma(w, dz, ez);
         }
     }
+    const long long mine = (blockIdx.x * (long long)PPB) / kVerletBlock * kVerletBlock;
+    const int self = (int)(i - mine);
     for (long long t0 = 0; t0 < A.n; t0 += kVerletBlock) {
         const int cnt = (int)min((long long)kVerletBlock, A.n - t0);
         __syncthreads();
         if (threadIdx.x < cnt)
             dtile[threadIdx.x] = A.in[t0 + threadIdx.x];
         __syncthreads();
-        if (t0 == blockIdx.x * (long long)kVerletBlock)
-            dyn_tile<T, true>(dtile, cnt, threadIdx.x, rx, ry, rz, ex, ey, ez, bx, by, bz);
+        if (t0 == mine)
+            dyn_tile<T, TPP, true>(dtile, cnt, self, t, rx, ry, rz, ex, ey, ez, bx, by, bz);
         else
-            dyn_tile<T, false>(dtile, cnt, -1, rx, ry, rz, ex, ey, ez, bx, by, bz);
+            dyn_tile<T, TPP, false>(dtile, cnt, -1, t, rx, ry, rz, ex, ey, ez, bx, by, bz);
     }
-    if (!own)
+    ex = lanes_sum<TPP>(ex);
+    ey = lanes_sum<TPP>(ey);
+    ez = lanes_sum<TPP>(ez);
+    bx = lanes_sum<TPP>(bx);
+    by = lanes_sum<TPP>(by);
+    bz = lanes_sum<TPP>(bz);
+    if (!own || t != 0)
         return;
     const T K = (T)kElectroK, MK = (T)kMagnetoK;
     ex *= K;
@@ -199,7 +226,8 @@ int verlet(T *dyn, T *accel, size_t n, const T *charges, size_t p, const T *box_
     if (opt)
         o = *opt;
     if (o.device_ptrs && (((uintptr_t)dyn % alignof(Dyn<T>)) ||
-                          (((uintptr_t)accel | (uintptr_t)charges) % sizeof(T))))
+                          ((uintptr_t)charges % alignof(Q4<T>)) ||
+                          ((uintptr_t)accel % sizeof(T))))
         return EM_ERR_ARG;
     int code = EM_OK;
     DevCtx *cp = get_ctx(&code);
@@ -244,13 +272,26 @@ int verlet(T *dyn, T *accel, size_t n, const T *charges, size_t p, const T *box_
         A.hi[k] = box_max[k];
     }
     A.dt = dt;
-    const unsigned grid = (unsigned)((n + kVerletBlock - 1) / kVerletBlock);
+    // lanes per particle: the caller's (opt->threads_per_line), else enough
+    // threads for about 48 warps per SM
+    const size_t want = (size_t)c.nsm * 48 * 32;
+    int tpp = n * 2 <= want ? 4 : n <= want ? 2 : 1;
+    if (o.threads_per_line)
+        tpp = o.threads_per_line;
+    if (tpp != 1 && tpp != 2 && tpp != 4)
+        return EM_ERR_ARG;
+    const unsigned grid = (unsigned)((n * tpp + kVerletBlock - 1) / kVerletBlock);
     if (e == cudaSuccess)
         e = cudaEventRecord(c.ev0, s);
     for (size_t k = 0; k < steps && e == cudaSuccess; ++k) {
         A.in = buf[k & 1];
         A.out = buf[(k + 1) & 1];
-        verlet_kernel<T><<<grid, kVerletBlock, 0, s>>>(A);
+        if (tpp == 4)
+            verlet_kernel<T, 4><<<grid, kVerletBlock, 0, s>>>(A);
+        else if (tpp == 2)
+            verlet_kernel<T, 2><<<grid, kVerletBlock, 0, s>>>(A);
+        else
+            verlet_kernel<T, 1><<<grid, kVerletBlock, 0, s>>>(A);
         count_launch(1);
         e = cudaGetLastError();
     }

@@ -384,10 +384,11 @@ def calc_field_multi(x, y, z, charges, n, devices, resolution=1.0,
 
 
 def verlet_step(dyn, accel, charges, box_min, box_max, dt, steps=1,
-                stream=None):
+                stream=None, lanes_per_particle=0):
     """Velocity-Verlet steps of moving charges (em_verlet_step_*), in place.
     dyn (n, 8) {x, y, z, q, vx, vy, vz, m}, accel (n, 3), charges (p, 4):
     numpy arrays, or CUDA tensors (then on the current torch stream).
+    lanes_per_particle: 1, 2 or 4 (0: the library's choice).
     Returns the perf record."""
     lib = _capi.load()
     dev = _is_torch(dyn) and dyn.is_cuda
@@ -400,6 +401,7 @@ def verlet_step(dyn, accel, charges, box_min, box_max, dt, steps=1,
     lo = np.ascontiguousarray(box_min, npt)
     hi = np.ascontiguousarray(box_max, npt)
     o = _capi.EmOptions()
+    o.threads_per_line = lanes_per_particle
     if dev:
         import torch
         o.device_ptrs = 1

@@ -337,7 +337,9 @@ EM_API int em_calc_field_multi_f64(const int *devices, size_t ndevices,
  * and the other particles of q r / |r|^3 at r'; B = 1e-7 sum over the other
  * particles of q v x r / |r|^3; a = q (E + v' x B) / m; v = v' + a dt/2;
  * then reflection off the walls of [box_min, box_max].  Returns 1 for n == 0
- * (the reference's check).  Host pointers unless opt->device_ptrs. */
+ * (the reference's check).  opt->threads_per_line, if set, is the number of
+ * lanes that share a particle's sums (1, 2 or 4; default: enough to fill the
+ * GPU).  Host pointers unless opt->device_ptrs. */
 EM_API int em_verlet_step_f32(float *dyn, float *accel, size_t n,
                               const float *charges, size_t p,
                               const float *box_min, const float *box_max,

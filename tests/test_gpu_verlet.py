@@ -33,11 +33,12 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("n,p", [(1, 0), (200, 0), (300, 77), (1000, 1500)])
-def test_fp64_matches_restatement(em, gpu, n, p):
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4])
+def test_fp64_matches_restatement(em, gpu, n, p, lanes):
     dyn, acc, ch = system(n, p)
     ref_dyn, ref_acc = N.verlet_step(dyn, acc, ch, *BOX, 1e-4)
     d, a = dyn.copy(), acc.copy()
-    em.verlet_step(d, a, ch.copy(), *BOX, 1e-4)
+    em.verlet_step(d, a, ch.copy(), *BOX, 1e-4, lanes_per_particle=lanes)
     assert rel(a, ref_acc) <= 1e-12
     assert rel(d[:, :3], ref_dyn[:, :3]) <= 1e-14
     assert rel(d[:, 4:7], ref_dyn[:, 4:7]) <= 1e-12
