@@ -390,10 +390,32 @@ def main():
         "cpu_baseline": cpu,
     }
     line.update(extras)
+    line["metric_parts"] = metric_parts(value, extras)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def metric_parts(value, extras):
+    """The metric's parts in one place: the plain FP32 rate (`value`), the
+    mixed-precision tracer against it per pair (200 rows, no termination)
+    with its field error vs FP64, and the adjoint/forward time ratio."""
+    parts = {"plain_fp32_gpair_s": value}
+    prec = extras.get("precision", {})
+    if "mixed_vs_fp32" in prec:
+        mixed = prec.get("mixed", {}).get("field_err_vs_fp64") or {}
+        parts.update({"mixed_vs_plain_fp32": prec["mixed_vs_fp32"],
+                      "mixed_vs_fp64": prec.get("mixed_vs_fp64"),
+                      "mixed_field_err_median": mixed.get("median"),
+                      "mixed_field_err_max": mixed.get("max"),
+                      "mixed_frac_le_1e-6": mixed.get("frac_le_1e-6")})
+    adj = extras.get("adjoint", {})
+    if "stored" in adj:
+        parts["adjoint_over_forward"] = adj["stored"]["adjoint_over_forward"]
+        parts["adjoint_over_forward_checkpointed"] = (
+            adj["checkpoint"]["adjoint_over_forward"])
+    return parts
 
 
 def field_errors(em, torch, ch, V, F, ln, samples, seed):
