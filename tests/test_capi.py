@@ -65,3 +65,26 @@ def test_dropin_header_compiles_against_stand_in_types(tmp_path):
     # without a GPU the traced call reports EM_ERR_NO_DEVICE (13); with one
     # it succeeds; the argument-check calls return the reference's codes
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+REFERENCE = os.environ.get("EM_REFERENCE_DIR", "/root/reference")
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(
+    REFERENCE, "ElectroMag", "src", "CPU Implement.h")),
+    reason="reference tree not present")
+def test_dropin_against_reference_headers(tmp_path):
+    """The INTEGRATION.md forwards compile against the reference's own
+    headers, link against libemgb300.so and return its argument codes."""
+    src = os.path.join(ROOT, "tests", "dropin_reference_headers.cpp")
+    exe = tmp_path / "dropin_ref"
+    lib = os.path.join(ROOT, "electromag-with-cuda_gb300")
+    r = subprocess.run(["g++", "-std=c++11", src,
+                        "-I" + os.path.join(REFERENCE, "include"),
+                        "-I" + os.path.join(REFERENCE, "ElectroMag", "src"),
+                        "-I" + os.path.join(ROOT, "include"), "-L" + lib,
+                        "-lemgb300", "-Wl,-rpath," + lib, "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
