@@ -282,3 +282,37 @@ def test_no_charges_traces_a_zero_field(em, gpu, arith):
     v = np.stack([x, y, z]).reshape(3, 6, 64)
     assert np.array_equal(v[:, 0], seeds.T)
     assert np.all(np.isnan(v[:, 1:]))
+
+
+def test_indexing_beyond_two_to_the_31(em, gpu):
+    """524 288 lines x 5000 rows: 2.6e9 elements per component array (the
+    reference's largest presets reach 1e10).  The last lines' rows, stored
+    past element 2^31, equal a separate 64-line call with the same shape."""
+    torch = pytest.importorskip("torch")
+    free, _ = torch.cuda.mem_get_info()
+    n, rows = 524288, 5000
+    if free < 3 * n * rows * 4 + (4 << 30):
+        pytest.skip("not enough device memory")
+    rng = np.random.default_rng(8)
+    ch = np.zeros((64, 4), np.float32)
+    ch[:, :3] = rng.uniform(-50, 50, (64, 3))
+    ch[:, 3] = rng.uniform(1, 10, 64) * rng.choice([-1, 1], 64)
+    seeds = rng.uniform(-60, 60, (n, 3)).astype(np.float32)
+    shape = dict(threads_per_line=4, lines_per_thread=1)
+    dch = torch.from_numpy(ch).cuda()
+    X = [torch.empty(n * rows, dtype=torch.float32, device="cuda") for _ in range(3)]
+    for c in range(3):
+        X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c])).cuda()
+    rc, _ = em.calc_field(*X, dch, n, 1.0, True, **shape)
+    assert rc == 0
+    tail = np.arange(n - 64, n)
+    big = np.stack([X[c].view(rows, n)[:, tail].cpu().numpy() for c in range(3)])
+    del X
+    torch.cuda.empty_cache()
+    Y = [torch.zeros(64 * rows, dtype=torch.float32, device="cuda") for _ in range(3)]
+    for c in range(3):
+        Y[c][:64] = torch.from_numpy(np.ascontiguousarray(seeds[tail, c])).cuda()
+    rc, _ = em.calc_field(*Y, dch, 64, 1.0, True, **shape)
+    assert rc == 0
+    small = np.stack([Y[c].view(rows, 64).cpu().numpy() for c in range(3)])
+    assert np.array_equal(big, small)
