@@ -442,14 +442,15 @@ def field_errors(em, torch, ch, V, F, ln, samples, seed):
 
 
 def traced(em, torch, ch, seeds, steps, term, precision, want_field,
-           null_frac=0.0):
+           null_frac=0.0, refine="fp64"):
     dt = torch.float64 if precision == "fp64" else torch.float32
     em.trace_lines(seeds.to(dt), ch.to(dt), min(steps, 8), 1.0, term,
-                   precision=precision, null_frac=null_frac)  # warm-up
+                   precision=precision, null_frac=null_frac,
+                   refine=refine)  # warm-up
     torch.cuda.synchronize()
     out = em.trace_lines(seeds.to(dt), ch.to(dt), steps, 1.0, term,
                          precision=precision, want_field=want_field,
-                         null_frac=null_frac)
+                         null_frac=null_frac, refine=refine)
     torch.cuda.synchronize()
     perf = out["perf"]
     out["gpairs"] = perf.pairs / perf.time / 1e9 if perf.time > 0 else 0.0
@@ -457,18 +458,21 @@ def traced(em, torch, ch, seeds, steps, term, precision, want_field,
 
 
 def precision_block(em, torch, dev, name, steps, seed, samples, with_ratio):
-    """FP32 / mixed / FP64 runs of the extended method on one workload, with
-    throughput and field error vs FP64."""
+    """FP32 / mixed / double-float / FP64 runs of the extended method on one
+    workload, with throughput and field error vs FP64; the mixed mode also
+    with null_frac 0.05, its re-evaluations in FP64 or in double-float."""
     ch_np, seeds_np, _ = em.workloads.make(name, seed=seed)
     ch = torch.from_numpy(np.ascontiguousarray(ch_np, np.float32)).to(dev)
     seeds = torch.from_numpy(seeds_np.astype(np.float32)).to(dev)
     blk = {"workload": name, "lines": int(len(seeds_np)),
            "charges": int(len(ch_np)), "max_rows": steps,
            "term_radius": 0.5}
-    for prec, nf in (("fp32", 0.0), ("mixed", 0.0), ("mixed_nf0.05", 0.05),
-                     ("fp64", 0.0)):
+    for prec, nf, refine in (("fp32", 0.0, "fp64"), ("mixed", 0.0, "fp64"),
+                             ("mixed_nf0.05", 0.05, "fp64"),
+                             ("mixed_nf0.05_df64", 0.05, "df64"),
+                             ("df64", 0.0, "fp64"), ("fp64", 0.0, "fp64")):
         p = "mixed" if prec.startswith("mixed") else prec
-        out = traced(em, torch, ch, seeds, steps, 0.5, p, True, nf)
+        out = traced(em, torch, ch, seeds, steps, 0.5, p, True, nf, refine)
         ln = out["len"]
         cls = np.bincount(out["cls"].cpu().numpy(), minlength=3)
         errs = field_errors(em, torch, ch, out["vertices"], out["field"], ln,
@@ -485,12 +489,13 @@ def precision_block(em, torch, dev, name, steps, seed, samples, with_ratio):
     if with_ratio:
         # per-pair cost without termination: every line runs 200 rows
         r = {}
-        for p in ("fp32", "mixed", "fp64"):
+        for p in ("fp32", "mixed", "df64", "fp64"):
             out = traced(em, torch, ch, seeds, 200, 0.0, p, False)
             r[p] = out["gpairs"]
         blk["no_termination_200_rows_gpair_s"] = r
         blk["mixed_vs_fp32"] = r["mixed"] / r["fp32"]
         blk["mixed_vs_fp64"] = r["mixed"] / r["fp64"]
+        blk["df64_vs_fp64"] = r["df64"] / r["fp64"]
     return blk
 
 

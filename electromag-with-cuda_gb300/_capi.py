@@ -37,6 +37,9 @@ EM_PACK_SCALAR = 1
 EM_PACK_PAIRS = 2
 EM_PREC_FP32 = 0
 EM_PREC_MIXED = 1
+EM_PREC_DF64 = 2
+EM_REFINE_FP64 = 0
+EM_REFINE_DF64 = 1
 EM_TERM_STEPS = 0
 EM_TERM_CHARGE = 1
 EM_TERM_NULL = 2
@@ -64,7 +67,7 @@ class EmOptions(ctypes.Structure):
                 ("force_streamed", I), ("pack", I),
                 ("lines_per_thread", I), ("precision", I),
                 ("null_frac", D), ("deterministic", I),
-                ("adjoint_checkpoint", I)]
+                ("adjoint_checkpoint", I), ("refine", I)]
 
 
 _SIGNATURES = {

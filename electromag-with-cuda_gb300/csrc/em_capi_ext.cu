@@ -38,10 +38,15 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     em_options o{};
     if (opt)
         o = *opt;
-    const int mode = o.precision == EM_PREC_MIXED ? EXT_MIXED : EXT_FAST;
-    if (o.precision != EM_PREC_FP32 && o.precision != EM_PREC_MIXED)
+    const int mode = o.precision == EM_PREC_MIXED  ? EXT_MIXED
+                     : o.precision == EM_PREC_DF64 ? EXT_DF64
+                                                   : EXT_FAST;
+    if (o.precision != EM_PREC_FP32 && o.precision != EM_PREC_MIXED &&
+        o.precision != EM_PREC_DF64)
         return EM_ERR_ARG;
-    if (mode == EXT_MIXED && sizeof(T) != 4)
+    if (mode != EXT_FAST && sizeof(T) != 4)
+        return EM_ERR_ARG;
+    if (o.refine != EM_REFINE_FP64 && o.refine != EM_REFINE_DF64)
         return EM_ERR_ARG;
     if (!(term_radius >= 0) || !(o.null_frac >= 0))
         return EM_ERR_ARG;
@@ -179,6 +184,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     prm.stages = cfg.stages;
     prm.resident = cfg.resident;
     prm.regroup = o.deterministic ? 0 : 1;
+    prm.refine_df64 = o.refine == EM_REFINE_DF64 ? 1 : 0;
     prm.err = c.err;
 
     e = cudaEventRecord(c.ev0, s);

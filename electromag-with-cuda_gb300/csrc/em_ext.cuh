@@ -156,6 +156,135 @@ __device__ __forceinline__ void field_fp64(const float4 *charges, int count, int
     }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic (a value is h + l, two FP32 words, about 48 bits):
+// error-free sums and products by the classical transformations (Knuth's
+// two-sum, Dekker's fast two-sum, the FMA two-product), every operation an
+// explicitly rounded intrinsic so nothing is contracted.  The evaluation
+// point is an FP32 vertex, so r = p - c is exact as a pair; the pair term
+// q r / |r|^3 is formed to about 2^-42 relative, on the FP32 pipes only
+// (GB300 runs FP64 at 1/64 of the FP32 rate).
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ DF df_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float ap = __fsub_rn(s, bp);
+    return {s, __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp))};
+}
+
+// |a| >= |b| (or a = 0)
+__device__ __forceinline__ DF df_fast(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ DF df_sqr(DF a)
+{
+    const float p = __fmul_rn(a.h, a.h);
+    float e = __fmaf_rn(a.h, a.h, -p);
+    e = __fmaf_rn(__fadd_rn(a.h, a.h), a.l, e);
+    return df_fast(p, e);
+}
+
+__device__ __forceinline__ DF df_mul(DF a, DF b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return df_fast(p, e);
+}
+
+__device__ __forceinline__ DF df_mul_f(DF a, float b)
+{
+    const float p = __fmul_rn(a.h, b);
+    float e = __fmaf_rn(a.h, b, -p);
+    e = __fmaf_rn(a.l, b, e);
+    return df_fast(p, e);
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+    const DF s = df_two_sum(a.h, b.h);
+    return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+
+// q r / |r|^3 for the FP32 point p and charge c, each component a DF; r2h
+// gets |r|^2 rounded to FP32 (for the nearest-negative test).
+__device__ __forceinline__ void df_pair(float px, float py, float pz, const float4 &c, DF &tx,
+                                        DF &ty, DF &tz, float &r2h)
+{
+    const DF dx = df_two_sum(px, -c.x), dy = df_two_sum(py, -c.y), dz = df_two_sum(pz, -c.z);
+    const DF r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+    r2h = r2.h;
+    // r^-1/2: the FP32 estimate, then one Newton step on the double-float
+    // residual h = 1 - r2 y0^2 (1 - t.h is exact: t.h is within 2^-21 of 1)
+    const float y0 = rsqrt_fast(r2.h);
+    const DF y2 = {__fmul_rn(y0, y0), __fmaf_rn(y0, y0, -__fmul_rn(y0, y0))};
+    const DF t = df_mul(r2, y2);
+    const float hres = __fsub_rn(__fsub_rn(1.0f, t.h), t.l);
+    const DF inv = df_fast(y0, __fmul_rn(__fmul_rn(y0, 0.5f), hres));
+    const DF s = df_mul_f(df_mul(df_sqr(inv), inv), c.w);
+    tx = df_mul(s, dx);
+    ty = df_mul(s, dy);
+    tz = df_mul(s, dz);
+}
+
+// The compensated accumulator takes a double-float term: its high word with
+// a two-sum, its low word added to the low sum.
+__device__ __forceinline__ void cf_add_df(CF &a, DF v)
+{
+    float e;
+    two_sum(a.h, v.h, a.h, e);
+    a.l = __fadd_rn(a.l, __fadd_rn(e, v.l));
+}
+
+// Double-float pairs over shared-memory records [0, count), lane t of TPL;
+// [0, jneg) are negative charges (nearest one tracked).
+template <int TPL>
+__device__ __forceinline__ void pairs_df64(const float4 *tile, int jneg, int count, int t,
+                                           float px, float py, float pz, CF &hx, CF &hy, CF &hz,
+                                           float &dneg)
+{
+#pragma unroll 2
+    for (int j = t; j < count; j += TPL) {
+        DF tx, ty, tz;
+        float r2h;
+        df_pair(px, py, pz, tile[j], tx, ty, tz, r2h);
+        if (j < jneg)
+            dneg = fminf(dneg, r2h);
+        cf_add_df(hx, tx);
+        cf_add_df(hy, ty);
+        cf_add_df(hz, tz);
+    }
+}
+
+// Double-float field at an FP32 point from the staged records in global
+// memory, lane t of TPL (summed later across the group), returned in FP64.
+template <int TPL>
+__device__ __forceinline__ void field_df64(const float4 *charges, int count, int t, float px,
+                                           float py, float pz, double &ax, double &ay,
+                                           double &az)
+{
+    CF hx, hy, hz;
+    for (int j = t; j < count; j += TPL) {
+        DF tx, ty, tz;
+        float r2h;
+        df_pair(px, py, pz, charges[j], tx, ty, tz, r2h);
+        cf_add_df(hx, tx);
+        cf_add_df(hy, ty);
+        cf_add_df(hz, tz);
+    }
+    ax += (double)hx.h + (double)hx.l;
+    ay += (double)hy.h + (double)hy.l;
+    az += (double)hz.h + (double)hz.l;
+}
+
 template <class T, int TPL>
 __device__ __forceinline__ T group_min(T v)
 {
@@ -231,6 +360,8 @@ __device__ __forceinline__ void tile_pairs(int tg, const Rec *tile, int jn, int 
 #define EM_TILE_PAIRS(G)                                                                       \
     if constexpr (MODE == EXT_MIXED)                                                           \
         pairs_mixed<G>(tile, jn, count, t, st.px, st.py, st.pz, hx, hy, hz, dneg, dall);       \
+    else if constexpr (MODE == EXT_DF64)                                                       \
+        pairs_df64<G>(tile, jn, count, t, st.px, st.py, st.pz, hx, hy, hz, dneg);              \
     else                                                                                       \
         pairs_fast<G>(tile, jn, count, t, st.px, st.py, st.pz, ax, ay, az, dneg);
     switch (tg) {
@@ -247,7 +378,7 @@ __device__ __forceinline__ void combine_group(int tg, T &ax, T &ay, T &az, T &dn
                                               CF &hx, CF &hy, CF &hz)
 {
 #define EM_COMBINE(G)                                                                          \
-    if constexpr (MODE == EXT_MIXED) {                                                         \
+    if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {                                     \
         group_two_sum<G>(hx);                                                                  \
         group_two_sum<G>(hy);                                                                  \
         group_two_sum<G>(hz);                                                                  \
@@ -268,6 +399,25 @@ __device__ __forceinline__ void combine_group(int tg, T &ax, T &ay, T &az, T &dn
     default: { EM_COMBINE(32) } break;
     }
 #undef EM_COMBINE
+}
+
+__device__ __forceinline__ void df64_field_group(int tg, const float4 *charges, int count, int t,
+                                                 float px, float py, float pz, double &fx,
+                                                 double &fy, double &fz, bool redo)
+{
+#define EM_DF64(G)                                                                             \
+    if (redo)                                                                                  \
+        field_df64<G>(charges, count, t, px, py, pz, fx, fy, fz);                              \
+    fx = group_sum<double, G>(fx);                                                             \
+    fy = group_sum<double, G>(fy);                                                             \
+    fz = group_sum<double, G>(fz);
+    switch (tg) {
+    case 4: { EM_DF64(4) } break;
+    case 8: { EM_DF64(8) } break;
+    case 16: { EM_DF64(16) } break;
+    default: { EM_DF64(32) } break;
+    }
+#undef EM_DF64
 }
 
 __device__ __forceinline__ void fp64_field_group(int tg, const float4 *charges, int count, int t,

@@ -67,6 +67,7 @@ template <class T> struct RefTraceParams {
 enum ExtMode : int {
     EXT_FAST = 0,  // T arithmetic throughout (float, or double = the FP64 path)
     EXT_MIXED = 1, // FP32 pairs + corrected inv^3 + compensation, FP64 position
+    EXT_DF64 = 2,  // double-float pairs (two FP32 words), FP64 position and step
 };
 // termination classes written by the kernel (same values as EM_TERM_*)
 constexpr int EM_TERM_STEPS_DEV = 0;
@@ -89,6 +90,7 @@ template <class T> struct ExtParams {
     unsigned long long *next_line, *evals, *refines;
     int p_pad, n_tiles, tile_recs, stages, resident;
     int regroup;                    // widen lane groups once the queue is dry
+    int refine_df64;                // mixed: re-evaluate nulls in double-float
     int *err;
 };
 

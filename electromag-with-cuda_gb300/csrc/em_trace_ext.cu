@@ -26,7 +26,12 @@
 //              to first order), two-sum compensated accumulation across
 //              chunks of 64 charges and across lanes, the line position in
 //              FP64, and an FP64 re-evaluation of the whole field where
-//              |E| < null_frac * (largest single contribution bound).
+//              |E| < null_frac * (largest single contribution bound)
+//              (in double-float instead with refine_df64).
+//   EXT_DF64   T = float: double-float pairs (two FP32 words each, about
+//              48 bits; the FP32 vertex makes r = p - c exact), compensated
+//              sums, the field and the step in FP64, the position in FP64:
+//              FP64-class fields on the FP32 pipes.
 #include "em_device.cuh"
 #include "em_ext.cuh"
 #include "em_internal.h"
@@ -326,19 +331,35 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         ax = mul_rn(ax, K);
         ay = mul_rn(ay, K);
         az = mul_rn(az, K);
+        // double-float mode: the field in FP64 (the two words of each sum)
+        double Edx = 0, Edy = 0, Edz = 0;
+        if constexpr (MODE == EXT_DF64) {
+            Edx = ((double)hx.h + (double)hx.l) * kElectroK;
+            Edy = ((double)hy.h + (double)hy.l) * kElectroK;
+            Edz = ((double)hz.h + (double)hz.l) * kElectroK;
+            ax = (T)Edx;
+            ay = (T)Edy;
+            az = (T)Edz;
+        }
 
         if constexpr (MODE == EXT_MIXED) {
             // near a null |E| is far below its largest term and the FP32 sum
-            // loses its digits: redo the field in FP64 there
+            // loses its digits: redo the field in FP64 there (or in
+            // double-float, on the FP32 pipes, with refine_df64)
             const float bound = qabs_max * (float)kElectroK / dall;
             const float e2 = ax * ax + ay * ay + az * az;
             const float lim2 = (float)P.null_frac * bound;
             const bool redo = live && !(e2 >= lim2 * lim2);
             if (__any_sync(0xffffffffu, redo)) {
                 double fx = 0, fy = 0, fz = 0;
-                fp64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
-                                 (double)(float)st.px, (double)(float)st.py,
-                                 (double)(float)st.pz, fx, fy, fz, redo);
+                if (P.refine_df64)
+                    df64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
+                                     (float)st.px, (float)st.py, (float)st.pz, fx, fy, fz,
+                                     redo);
+                else
+                    fp64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad,
+                                     t, (double)(float)st.px, (double)(float)st.py,
+                                     (double)(float)st.pz, fx, fy, fz, redo);
                 if (redo) {
                     ax = (T)(fx * kElectroK);
                     ay = (T)(fy * kElectroK);
@@ -362,9 +383,23 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
                 const T r0x = ld_seed(P.x + line), r0y = ld_seed(P.y + line),
                         r0z = ld_seed(P.z + line);
                 T sx, sy, sz, k2;
-                step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
                 T nx, ny, nz;
-                if constexpr (MODE == EXT_MIXED) {
+                if constexpr (MODE == EXT_DF64) {
+                    // the step in FP64 from the FP64 field
+                    double dsx, dsy, dsz, dk2;
+                    step_vector<double>(Edx, Edy, Edz, (double)r0x, (double)r0y, (double)r0z,
+                                        P.resolution, dsx, dsy, dsz, dk2);
+                    k2 = (T)dk2;
+                    if (dk2 > 0.0 && !(k2 > T(0)))
+                        k2 = T(1); // a positive FP64 |E|^2 below the FP32 range
+                    st.dx += dsx;
+                    st.dy += dsy;
+                    st.dz += dsz;
+                    nx = (T)st.dx;
+                    ny = (T)st.dy;
+                    nz = (T)st.dz;
+                } else if constexpr (MODE == EXT_MIXED) {
+                    step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
                     st.dx += (double)sx;
                     st.dy += (double)sy;
                     st.dz += (double)sz;
@@ -372,6 +407,7 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
                     ny = (T)st.dy;
                     nz = (T)st.dz;
                 } else {
+                    step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
                     nx = add_rn(st.px, sx);
                     ny = add_rn(st.py, sy);
                     nz = add_rn(st.pz, sz);
@@ -460,6 +496,8 @@ template <>
 cudaError_t launch_ext_trace<float>(const ExtParams<float> &p, const LaunchCfg &cfg, int mode,
                                     cudaStream_t stream)
 {
+    if (mode == EXT_DF64)
+        return launch_ext_mode<float, EXT_DF64>(p, cfg, stream);
     return mode == EXT_MIXED ? launch_ext_mode<float, EXT_MIXED>(p, cfg, stream)
                              : launch_ext_mode<float, EXT_FAST>(p, cfg, stream);
 }

@@ -161,19 +161,24 @@ def field(points, charges, *, arith="fast", rule="sse", stream=None):
     return out.T
 
 
-_PREC = {"fp32": _capi.EM_PREC_FP32, "mixed": _capi.EM_PREC_MIXED}
+_PREC = {"fp32": _capi.EM_PREC_FP32, "mixed": _capi.EM_PREC_MIXED,
+         "df64": _capi.EM_PREC_DF64}
+_REFINE = {"fp64": _capi.EM_REFINE_FP64, "df64": _capi.EM_REFINE_DF64}
 
 
 def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
                 steps_per_line=None, precision="fp32", want_field=False,
                 threads_per_line=0, warps_per_cta=0, tile_charges=0,
                 force_streamed=False, null_frac=0.0, deterministic=False,
-                stream=None):
+                refine="fp64", stream=None):
     """Extended method (seeded lines, termination, step limits).
 
     seeds (n, 3), charges (p, 4): numpy arrays (host entry point) or CUDA
     torch tensors (device entry point, current stream).  precision: "fp32",
-    "mixed" (FP32 pairs, FP64 positions and near-null fields) or "fp64".
+    "mixed" (FP32 pairs, FP64 positions and near-null fields; refine: the
+    arithmetic of those re-evaluations, "fp64" or "df64"), "df64"
+    (double-float pairs on the FP32 pipes, FP64 field and positions) or
+    "fp64".
     Returns a dict with vertices (3, max_steps, n), len (n,), cls (n,),
     field (3, max_steps, n) when want_field, and perf.
     """
@@ -188,6 +193,7 @@ def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
     o.force_streamed = int(bool(force_streamed))
     o.null_frac = null_frac
     o.deterministic = int(bool(deterministic))
+    o.refine = _REFINE[refine]
     perf = _capi.EmPerf()
     fn = lib.em_trace_lines_f64 if f64 else lib.em_trace_lines_f32
     if _is_torch(seeds):

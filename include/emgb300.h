@@ -93,7 +93,8 @@ typedef struct em_options {
     int force_streamed;   /* 1: stream charge tiles even if they fit          */
     int pack;             /* EM_PACK_*: pair loop form for fast FP32         */
     int lines_per_thread; /* 0: automatic; 1 or 2 (fast arithmetic only)     */
-    int precision;        /* em_trace_lines_f32: EM_PREC_FP32 or EM_PREC_MIXED */
+    int precision;        /* em_trace_lines_f32: EM_PREC_FP32, EM_PREC_MIXED
+                             or EM_PREC_DF64                                 */
     double null_frac;     /* mixed: FP64 re-evaluation where |E| is below this
                              fraction of the largest single contribution
                              (0: 1e-4)                                       */
@@ -106,6 +107,9 @@ typedef struct em_options {
                              field at every vertex (12 more bytes per vertex);
                              1 keeps only the vertices and recomputes the
                              field per 64-row segment                        */
+    int refine;           /* mixed precision: EM_REFINE_FP64 (default) or
+                             EM_REFINE_DF64, the arithmetic of the field
+                             re-evaluated near nulls                         */
 } em_options;
 
 /* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
@@ -113,6 +117,12 @@ typedef struct em_options {
 #define EM_PREC_MIXED 1   /* FP32 pairs with a Newton-corrected inv^3,
                              compensated sums, FP64 positions, FP64 field
                              near nulls                                      */
+#define EM_PREC_DF64 2    /* double-float pairs (two FP32 words, ~48 bits) on
+                             the FP32 pipes, FP64 field, step and positions:
+                             FP64-class fields at several times the native
+                             FP64 rate of GB300                              */
+#define EM_REFINE_FP64 0  /* mixed: re-evaluate near nulls in FP64           */
+#define EM_REFINE_DF64 1  /* mixed: re-evaluate near nulls in double-float   */
 
 /* ---- termination classes of the extended tracer --------------------------- */
 #define EM_TERM_STEPS 0   /* reached its step limit                          */

@@ -177,3 +177,56 @@ def test_regrouping_tail_agrees_and_is_faster(em, gpu, orc):
         err = np.abs(A[:, :m, i] - B[:, :m, i]) / np.maximum(np.abs(A[:, :m, i]), 1)
         assert err.max() <= VERTEX_RTOL
     assert b["perf"].time < a["perf"].time
+
+
+def _fields_at_vertices(out, step=4):
+    V, F, gl = out["vertices"], out["field"], out["len"]
+    pts, fld = [], []
+    for i in range(0, V.shape[2], step):
+        m = gl[i] - 1  # rows with an evaluated field that led to a step
+        pts.append(V[:, :m, i].T)
+        fld.append(F[:, :m, i].T)
+    return (np.concatenate(pts).astype(np.float64),
+            np.concatenate(fld).astype(np.float64))
+
+
+def test_df64_field_is_the_fp64_field_rounded(em, gpu, orc, ext_case):
+    """Double-float mode: the stored (FP32) field equals the FP64 field at
+    the same point to FP32 rounding at every vertex — where the mixed mode
+    reaches 1e-5 near cancellations."""
+    ch, seeds, _, _ = ext_case
+    out = em.trace_lines(seeds, ch, 200, 1.0, 0.5, precision="df64",
+                         want_field=True)
+    pts, fld = _fields_at_vertices(out)
+    e64 = orc.field_f64(pts, ch.astype(np.float64))
+    rel = np.linalg.norm(fld - e64, axis=1) / np.linalg.norm(e64, axis=1)
+    assert rel.max() <= 2e-7, rel.max()
+
+
+def test_df64_matches_fp64_oracle(em, gpu, ext_case):
+    ch, seeds, steps, ref = ext_case
+    out = em.trace_lines(seeds, ch, steps, 1.0, 0.5, precision="df64")
+    agree, vok, gl, _ = compare(out, ref)
+    assert agree >= CLASS_AGREE, agree
+    assert vok >= CLASS_AGREE, vok
+    assert np.all((gl >= 1) & (gl <= steps))
+
+
+def test_mixed_refinement_in_df64_equals_fp64(em, gpu, ext_case):
+    """Every vertex re-evaluated (null_frac far above 1): the double-float
+    and FP64 re-evaluations round to the same FP32 field almost everywhere
+    and never differ by more than one rounding."""
+    ch, seeds, _, _ = ext_case
+    runs = [em.trace_lines(seeds[:256], ch, 60, 1.0, 0.5, precision="mixed",
+                           want_field=True, null_frac=1e30, refine=r,
+                           deterministic=True)
+            for r in ("fp64", "df64")]
+    assert runs[0]["perf"].fp64_refines == runs[1]["perf"].fp64_refines > 0
+    assert np.array_equal(runs[0]["len"], runs[1]["len"])
+    pa, fa = _fields_at_vertices(runs[0], 1)
+    pb, fb = _fields_at_vertices(runs[1], 1)
+    assert np.array_equal(pa, pb)
+    same = (fa == fb).all(axis=1).mean()
+    rel = np.linalg.norm(fa - fb, axis=1) / np.linalg.norm(fa, axis=1)
+    assert same >= 0.999, same
+    assert rel.max() <= 1.2e-7, rel.max()
