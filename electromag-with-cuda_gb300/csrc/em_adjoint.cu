@@ -23,7 +23,7 @@
 // its rows backwards; lane l of warp w owns charges k*32W + 32w + l (k < CPL)
 // and keeps their four gradient sums in registers across all the rows and
 // lines it processes, flushing them every 512 rows into compensated (hi, lo)
-// partials of its team.  Each pair is formed once (26 FP32 ops + one rsqrt)
+// partials of its team.  Each pair is formed once (23 FP32 ops + one rsqrt)
 // instead of twice.  Per block of 32 rows, lane l prepares row (top - l):
 // u, lam/|E'|, the vertex and 2 (v - t); each row then takes them from that
 // lane by shuffle.
@@ -58,8 +58,12 @@ __device__ __forceinline__ float lane_sum(float v)
     return v;
 }
 
-// Loss sum (v - t)^2 over all vertices: one FP64 partial per CTA (part),
-// summed in CTA order by adj_loss_sum_kernel, so the loss repeats bit for bit.
+// Loss sum |v - t|^2 over all vertices: each vertex's term in FP32 (within
+// about 3e-7 of its exact value; the terms are positive, so the sum keeps
+// that relative bound), summed in FP64 (GB300 runs FP64 at 1/64 of the FP32
+// rate, so one FP64 add per vertex keeps the kernel at memory speed).  One
+// FP64 partial per CTA (part), summed in a fixed order by
+// adj_loss_sum_kernel, so the loss repeats bit for bit.
 __global__ void __launch_bounds__(256) adj_loss_kernel(const float *x, const float *y,
                                                        const float *z, const float *tx,
                                                        const float *ty, const float *tz,
@@ -68,9 +72,8 @@ __global__ void __launch_bounds__(256) adj_loss_kernel(const float *x, const flo
     double acc = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < elems;
          i += (size_t)gridDim.x * blockDim.x) {
-        const double dx = (double)x[i] - tx[i], dy = (double)y[i] - ty[i],
-                     dz = (double)z[i] - tz[i];
-        acc += dx * dx + dy * dy + dz * dz;
+        const float dx = x[i] - tx[i], dy = y[i] - ty[i], dz = z[i] - tz[i];
+        acc += (double)fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     }
     for (int o = 16; o; o >>= 1)
         acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -86,14 +89,17 @@ __global__ void __launch_bounds__(256) adj_loss_kernel(const float *x, const flo
     }
 }
 
+// One warp: lane l sums partials l, l + 32, ... in order, then a fixed
+// butterfly.
 __global__ void adj_loss_sum_kernel(const double *part, int n, double *loss)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0;
-        for (int i = 0; i < n; ++i)
-            s += part[i];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += 32)
+        s += part[i];
+    for (int o = 16; o; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0)
         *loss = s;
-    }
 }
 
 // Backward over rows [s_lo, s_hi) of one segment for every line.
@@ -279,16 +285,104 @@ __global__ void __launch_bounds__(kChargeThreads) adj_charge_kernel(const AdjPar
     }
 }
 
-// E' = E/K at the stored vertices of rows [s_lo, s_hi), written at row
-// (s - f_row0): the forward's pair loop, lane order and reduction (TPL = 8,
-// charges t, t+8, ...), so the bits equal the forward's.
-__global__ void __launch_bounds__(1024, 1) adj_field_kernel(const AdjParams P, int s_lo, int s_hi)
+// One lane's chain of the forward's TPL = 8 charge split: charges t8,
+// t8 + 8, ... summed in order into a zero start, for PPT vertices at once
+// (each broadcast charge load feeds PPT pairs).  The pair is the forward's
+// fast form (ref_trace_kernel, ARITH_FAST).
+template <int PPT>
+__device__ __forceinline__ void lane_chain(const float4 *tiles, int p_pad, int t8,
+                                           const float (&px)[PPT], const float (&py)[PPT],
+                                           const float (&pz)[PPT], float (&a)[PPT][3])
 {
-    constexpr int TPL = kAdjTpl, LG = 32 / TPL;
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+        a[k][0] = a[k][1] = a[k][2] = 0.0f;
+#pragma unroll 4
+    for (int j = t8; j < p_pad; j += 8) {
+        const float4 c = tiles[j];
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+            const float dx = px[k] - c.x, dy = py[k] - c.y, dz = pz[k] - c.z;
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float inv = rsqrt_fast(r2);
+            const float sc = (c.w * inv) * (inv * inv);
+            a[k][0] = fmaf(sc, dx, a[k][0]);
+            a[k][1] = fmaf(sc, dy, a[k][1]);
+            a[k][2] = fmaf(sc, dz, a[k][2]);
+        }
+    }
+}
+
+template <int PPT>
+__device__ __forceinline__ void add_into(float (&a)[PPT][3], const float (&b)[PPT][3])
+{
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            a[k][c] = a[k][c] + b[k][c];
+}
+
+// E' at PPT vertices (flat element indices e[k]; ok[k] false for none):
+// the eight lane sums of the forward, combined as its xor butterfly over
+// offsets 4, 2, 1 gives them, ((a0+a4) + (a2+a6)) + ((a1+a5) + (a3+a7))
+// (float addition commutes, so every lane of the butterfly holds these
+// bits).  Chains run in the order 0, 4, 2, 6, 1, 5, 3, 7 so at most four
+// partial sums are live.
+template <int PPT>
+__device__ __forceinline__ void points_field(const AdjParams &P, const float4 *tiles,
+                                             const size_t (&e)[PPT], const bool (&ok)[PPT],
+                                             size_t out_shift)
+{
+    float px[PPT], py[PPT], pz[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        px[k] = ok[k] ? P.x[e[k]] : 0.0f;
+        py[k] = ok[k] ? P.y[e[k]] : 0.0f;
+        pz[k] = ok[k] ? P.z[e[k]] : 0.0f;
+    }
+    float A[PPT][3], B[PPT][3], C[PPT][3], D[PPT][3];
+    lane_chain<PPT>(tiles, P.p_pad, 0, px, py, pz, A);
+    lane_chain<PPT>(tiles, P.p_pad, 4, px, py, pz, B);
+    add_into<PPT>(A, B); // a0 + a4
+    lane_chain<PPT>(tiles, P.p_pad, 2, px, py, pz, B);
+    lane_chain<PPT>(tiles, P.p_pad, 6, px, py, pz, C);
+    add_into<PPT>(B, C); // a2 + a6
+    add_into<PPT>(A, B);
+    lane_chain<PPT>(tiles, P.p_pad, 1, px, py, pz, B);
+    lane_chain<PPT>(tiles, P.p_pad, 5, px, py, pz, C);
+    add_into<PPT>(B, C); // a1 + a5
+    lane_chain<PPT>(tiles, P.p_pad, 3, px, py, pz, C);
+    lane_chain<PPT>(tiles, P.p_pad, 7, px, py, pz, D);
+    add_into<PPT>(C, D); // a3 + a7
+    add_into<PPT>(B, C);
+    add_into<PPT>(A, B);
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        if (ok[k]) {
+            const size_t o = e[k] - out_shift;
+            P.fx[o] = A[k][0];
+            P.fy[o] = A[k][1];
+            P.fz[o] = A[k][2];
+        }
+    }
+}
+
+// E' = E/K at the stored vertices of rows [s_lo, s_hi), written at row
+// (s - f_row0), with the bits of the forward's TPL = 8 sums (points_field).
+// Vertex-parallel: the rows' vertices are one contiguous run of the line
+// arrays; thread i of T takes elements i, i + T, ... in groups of
+// kFieldPts (one broadcast charge load per kFieldPts pairs), then one at a
+// time, so every thread's share differs by at most one vertex.
+constexpr int kFieldPts = 3;
+constexpr int kFieldThreads = 256;
+
+__global__ void __launch_bounds__(kFieldThreads, 3) adj_field_kernel(const AdjParams P, int s_lo,
+                                                                  int s_hi)
+{
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    float4 *tiles = reinterpret_cast<float4 *>(smem + 128);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, t = lane % TPL;
+    const float4 *tiles = reinterpret_cast<const float4 *>(smem + 128);
     const uint32_t b0 = smem_addr(bar);
     if (threadIdx.x == 0) {
         mbar_init(b0, 1);
@@ -301,43 +395,30 @@ __global__ void __launch_bounds__(1024, 1) adj_field_kernel(const AdjParams P, i
         const char *src = static_cast<const char *>(P.charges);
         constexpr uint32_t CH = 32768;
         for (uint32_t off = 0; off < bytes; off += CH)
-            bulk_g2s(smem_addr(tiles) + off, src + off, bytes - off < CH ? bytes - off : CH, b0);
+            bulk_g2s(smem_addr(smem + 128) + off, src + off, bytes - off < CH ? bytes - off : CH,
+                     b0);
     }
     if (!mbar_wait(b0, 0, P.err))
         return;
     const size_t n = (size_t)P.n;
-    const long long groups = (P.n + LG - 1) / LG;
-    const int nw = blockDim.x >> 5;
-    for (long long g = blockIdx.x + (long long)gridDim.x * warp; g < groups;
-         g += (long long)gridDim.x * nw) {
-        const long long line = g * LG + lane / TPL;
-        const bool own = line < P.n;
-        const long long l = own ? line : 0;
-        for (int s = s_lo; s < s_hi; ++s) {
-            const size_t i = (size_t)s * n + l;
-            const float vx = P.x[i], vy = P.y[i], vz = P.z[i];
-            float ex = 0, ey = 0, ez = 0;
-#pragma unroll 8
-            for (int j = t; j < P.p_pad; j += TPL) {
-                const float4 c = tiles[j];
-                const float dx = vx - c.x, dy = vy - c.y, dz = vz - c.z;
-                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                const float inv = rsqrt_fast(r2);
-                const float sc = (c.w * inv) * (inv * inv);
-                ex = fmaf(sc, dx, ex);
-                ey = fmaf(sc, dy, ey);
-                ez = fmaf(sc, dz, ez);
-            }
-            ex = lane_sum<TPL>(ex);
-            ey = lane_sum<TPL>(ey);
-            ez = lane_sum<TPL>(ez);
-            if (own && t == 0) {
-                const size_t fi = (size_t)(s - P.f_row0) * n + (size_t)line;
-                P.fx[fi] = ex;
-                P.fy[fi] = ey;
-                P.fz[fi] = ez;
-            }
+    const size_t first = (size_t)s_lo * n, last = (size_t)s_hi * n;
+    const size_t shift = (size_t)P.f_row0 * n;
+    const size_t T = (size_t)gridDim.x * blockDim.x;
+    size_t i = first + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (kFieldPts - 1) * T < last; i += kFieldPts * T) {
+        size_t e[kFieldPts];
+        bool ok[kFieldPts];
+#pragma unroll
+        for (int k = 0; k < kFieldPts; ++k) {
+            e[k] = i + k * T;
+            ok[k] = true;
         }
+        points_field<kFieldPts>(P, tiles, e, ok, shift);
+    }
+    for (; i < last; i += T) {
+        const size_t e[1] = {i};
+        const bool ok[1] = {true};
+        points_field<1>(P, tiles, e, ok, shift);
     }
 }
 
@@ -481,8 +562,10 @@ __global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const
                 const float mx = f * fmaf(-ux, ua, ax), my = f * fmaf(-uy, ua, ay),
                             mz = f * fmaf(-uz, ua, az);
                 const float m3x = -3.0f * mx, m3y = -3.0f * my, m3z = -3.0f * mz;
-                // G(r) mu = inv3 mu + w3 r, w3 = -3 (r.mu) / r^5
-                float s1 = 0, wx = 0, wy = 0, wz = 0;
+                // G(r) mu = inv3 h, h = mu + (d3 inv2) r with d3 = -3 r.mu:
+                // h feeds the charge's position sums and, times q inv3, the
+                // line's Jacobian-vector sum l
+                float lx = 0, ly = 0, lz = 0;
 #pragma unroll
                 for (int k = 0; k < CPL; ++k) {
                     const float4 c = ch[k * W * 32];
@@ -492,44 +575,54 @@ __global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const
                     const float inv2 = inv * inv;
                     const float inv3 = inv2 * inv;
                     const float d3 = fmaf(dz, m3z, fmaf(dy, m3y, dx * m3x));
-                    const float hd = d3 * inv3;
-                    const float w3 = hd * inv2;
-                    g[3][k] += hd;
-                    g[0][k] = fmaf(w3, dx, fmaf(inv3, mx, g[0][k]));
-                    g[1][k] = fmaf(w3, dy, fmaf(inv3, my, g[1][k]));
-                    g[2][k] = fmaf(w3, dz, fmaf(inv3, mz, g[2][k]));
-                    s1 = fmaf(c.w, inv3, s1);
-                    const float qw = c.w * w3;
-                    wx = fmaf(qw, dx, wx);
-                    wy = fmaf(qw, dy, wy);
-                    wz = fmaf(qw, dz, wz);
+                    const float t = d3 * inv2;
+                    const float hx = fmaf(t, dx, mx), hy = fmaf(t, dy, my), hz = fmaf(t, dz, mz);
+                    g[0][k] = fmaf(inv3, hx, g[0][k]);
+                    g[1][k] = fmaf(inv3, hy, g[1][k]);
+                    g[2][k] = fmaf(inv3, hz, g[2][k]);
+                    g[3][k] = fmaf(d3, inv3, g[3][k]);
+                    const float qi3 = c.w * inv3;
+                    lx = fmaf(qi3, hx, lx);
+                    ly = fmaf(qi3, hy, ly);
+                    lz = fmaf(qi3, hz, lz);
                 }
-#pragma unroll
-                for (int o = 16; o >= 1; o >>= 1) {
-                    s1 += __shfl_xor_sync(FULL, s1, o);
-                    wx += __shfl_xor_sync(FULL, wx, o);
-                    wy += __shfl_xor_sync(FULL, wy, o);
-                    wz += __shfl_xor_sync(FULL, wz, o);
+                // warp sums of (lx, ly, lz): halve the values a lane carries
+                // at offsets 16 and 8 (each lane sends the half its partner
+                // keeps; the fourth slot is empty), finish with three full
+                // levels, so lane 8i holds sum i; then broadcast
+                {
+                    const bool b16 = lane & 16, b8 = lane & 8;
+                    float k0 = b16 ? lz : lx, k1 = b16 ? 0.0f : ly;
+                    const float d0 = b16 ? lx : lz, d1 = b16 ? ly : 0.0f;
+                    k0 += __shfl_xor_sync(FULL, d0, 16);
+                    k1 += __shfl_xor_sync(FULL, d1, 16);
+                    float k = b8 ? k1 : k0;
+                    k += __shfl_xor_sync(FULL, b8 ? k0 : k1, 8);
+                    k += __shfl_xor_sync(FULL, k, 4);
+                    k += __shfl_xor_sync(FULL, k, 2);
+                    k += __shfl_xor_sync(FULL, k, 1);
+                    lx = __shfl_sync(FULL, k, 0);
+                    ly = __shfl_sync(FULL, k, 8);
+                    lz = __shfl_sync(FULL, k, 16);
                 }
                 if (W > 1) {
                     // team sum in warp order, identical in every warp; slots
                     // alternate by row parity so one barrier per row suffices
                     float4 *slot = red + (s & 1) * 4;
                     if (lane == 0)
-                        slot[warp] = make_float4(s1, wx, wy, wz);
+                        slot[warp] = make_float4(lx, ly, lz, 0.0f);
                     asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(32 * W) : "memory");
-                    s1 = wx = wy = wz = 0;
+                    lx = ly = lz = 0;
                     for (int w = 0; w < W; ++w) {
                         const float4 v = slot[team * W + w];
-                        s1 += v.x;
-                        wx += v.y;
-                        wy += v.z;
-                        wz += v.w;
+                        lx += v.x;
+                        ly += v.y;
+                        lz += v.z;
                     }
                 }
-                ax = (gxs + ax) + fmaf(s1, mx, wx);
-                ay = (gys + ay) + fmaf(s1, my, wy);
-                az = (gzs + az) + fmaf(s1, mz, wz);
+                ax = (gxs + ax) + lx;
+                ay = (gys + ay) + ly;
+                az = (gzs + az) + lz;
             }
             acc_rows += bh - bl;
             if (acc_rows >= kFlushRows) {
@@ -704,6 +797,15 @@ cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, i
     adj_init_kernel<<<(unsigned)((P.n + 255) / 256), 256, 0, stream>>>(P);
     count_launch(3);
     const int seg = P.seg;
+    int field_grid = nsm;
+    if (fused && !P.stored) {
+        int per_sm = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_field_kernel,
+                                                               kFieldThreads, smem)) !=
+            cudaSuccess)
+            return e;
+        field_grid = nsm * (per_sm > 0 ? per_sm : 1);
+    }
     if (fused) {
         if (P.stored) {
             if ((e = launch_fused(P, *fused, 0, P.rows - 1, stream)) != cudaSuccess)
@@ -713,7 +815,7 @@ cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, i
                 const int lo = std::max(0, hi - seg);
                 AdjParams Q = P;
                 Q.f_row0 = lo;
-                adj_field_kernel<<<nsm, 1024, smem, stream>>>(Q, lo, hi);
+                adj_field_kernel<<<field_grid, kFieldThreads, smem, stream>>>(Q, lo, hi);
                 count_launch(1);
                 if ((e = launch_fused(Q, *fused, lo, hi, stream)) != cudaSuccess)
                     return e;

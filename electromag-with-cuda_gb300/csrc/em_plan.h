@@ -58,47 +58,63 @@ inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 // Staged charge layout for a kernel arithmetic (stage_kernel's `paired`).
 inline int stage_layout(int arith) { return arith == ARITH_FAST2 ? 1 : 0; }
 
-// Relative cost of one line-group step for `tpl` threads per line: pair
-// work per lane plus the butterfly and the per-vertex step.
+// Relative cost of one line-group step for `tpl` threads per line and `kl`
+// lines per lane: pair work per lane (one charge load per kl pairs) plus
+// the butterfly and the per-vertex step.
 inline double group_step_cost(long long p, int tpl, int kl)
 {
     int lg = 0;
     for (int t = tpl; t > 1; t >>= 1)
         ++lg;
-    return kl * ((double)ceil_div(p, tpl) * 13.0 + 18.0 * lg + 120.0);
+    return kl * ((double)ceil_div(p, tpl) * (13.0 + 1.0 / kl) + 18.0 * lg + 120.0);
 }
 
-// Picks threads per line, compute warps per CTA and the grid for n lines
-// and p charges on a device with nsm SMs (one persistent CTA per SM).  The
-// model charges each SM sub-partition (4 per SM) for the warps it runs.
+// Issue efficiency with w warps on the busiest SM sub-partition: too few
+// warps cannot hide the FP32-pipe and MUFU latencies.  Fitted to measured
+// traces of 16 384 lines x 1024 charges over every (tpl, kl) shape.
+inline double smsp_efficiency(long long w)
+{
+    return w >= 4 ? 1.0 : w == 3 ? 0.95 : w == 2 ? 0.87 : 0.68;
+}
+
+// Picks threads per line, lines per lane, compute warps per CTA and the
+// grid for n lines and p charges on a device with nsm SMs (one persistent
+// CTA per SM).  The model charges each SM sub-partition (4 per SM) for the
+// warps it runs.  fixed_tpl / fixed_kl of 0 are searched; shapes are tried
+// from (8, 2) down and a later one must be 2 % cheaper to replace an
+// earlier one.
 inline void choose_shape(long long n, long long p, int nsm, int max_warps, int fixed_tpl,
-                         int kl, int *tpl_out, int *warps_out)
+                         int fixed_kl, int *tpl_out, int *kl_out, int *warps_out)
 {
     double best = 0;
-    int bt = 1, bw = 1;
-    for (int tpl = 1; tpl <= 8; tpl <<= 1) {
-        if (fixed_tpl && tpl != fixed_tpl)
+    int bt = 1, bk = 1, bw = 1;
+    for (int kl = 2; kl >= 1; --kl) {
+        if (fixed_kl && kl != fixed_kl)
             continue;
-        const long long lpw = kl * 32 / tpl;
-        const long long groups = ceil_div(n, lpw);
-        const long long grid = std::min<long long>(nsm, groups);
-        const long long gpc = ceil_div(groups, grid);
-        const int warps = (int)std::min<long long>(max_warps, gpc);
-        const long long rounds = ceil_div(gpc, warps);
-        const long long last = gpc - (rounds - 1) * warps;
-        double per_smsp = (double)(rounds - 1) * (double)ceil_div(warps, 4) +
-                          (double)ceil_div(last, 4);
-        // one warp per sub-partition cannot hide the FP32 pipe latency
-        if (ceil_div(warps, 4) < 2)
-            per_smsp *= 1.6;
-        const double t = per_smsp * group_step_cost(p, tpl, kl);
-        if (best == 0 || t < best * 0.98) {
-            best = t;
-            bt = tpl;
-            bw = warps;
+        for (int tpl = 8; tpl >= 1; tpl >>= 1) {
+            if (fixed_tpl && tpl != fixed_tpl)
+                continue;
+            const long long lpw = kl * 32 / tpl;
+            const long long groups = ceil_div(n, lpw);
+            const long long grid = std::min<long long>(nsm, groups);
+            const long long gpc = ceil_div(groups, grid);
+            const int warps = (int)std::min<long long>(max_warps, gpc);
+            const long long rounds = ceil_div(gpc, warps);
+            const long long last = gpc - (rounds - 1) * warps;
+            const double per_smsp = (double)(rounds - 1) * (double)ceil_div(warps, 4) +
+                                    (double)ceil_div(last, 4);
+            const double t = per_smsp * group_step_cost(p, tpl, kl) /
+                             smsp_efficiency(ceil_div(warps, 4));
+            if (best == 0 || t < best * 0.98) {
+                best = t;
+                bt = tpl;
+                bk = kl;
+                bw = warps;
+            }
         }
     }
     *tpl_out = bt;
+    *kl_out = bk;
     *warps_out = bw;
 }
 
@@ -120,19 +136,22 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
         arith = ARITH_FAST2;
     if (o.lines_per_thread < 0 || o.lines_per_thread > 2)
         return EM_ERR_ARG;
-    // lines per lane: 2 for the fast forms when the caller does not say (one
-    // charge load feeds two independent chains), 1 for exact arithmetic
-    int kl = 1;
-    if (arith != ARITH_EXACT)
-        kl = o.lines_per_thread ? o.lines_per_thread : 2;
+    // lines per lane: searched for the fast scalar form when the caller does
+    // not say (two lines share each charge load, one line doubles the warps
+    // for small line counts); 2 for packed pairs, 1 for exact arithmetic
+    int fixed_kl = 1;
+    if (arith == ARITH_FAST)
+        fixed_kl = o.lines_per_thread;
+    else if (arith == ARITH_FAST2)
+        fixed_kl = o.lines_per_thread ? o.lines_per_thread : 2;
     const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
-    int tpl = 1, warps = 1;
+    int tpl = 1, kl = 1, warps = 1;
     // resident if the padded set fits next to the barrier block
     const size_t gran_max = 16 * kUnroll;
     const size_t p_res = (p + gran_max - 1) / gran_max * gran_max;
     const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
-    choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, kl, &tpl,
-                 &warps);
+    choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, fixed_kl,
+                 &tpl, &kl, &warps);
     if (o.warps_per_cta)
         warps = std::min(o.warps_per_cta, resident ? 32 : 31);
     // records per padding granule: every lane gets whole unrolled groups

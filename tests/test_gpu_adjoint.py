@@ -73,6 +73,28 @@ def test_adjoint_stored_and_checkpoint_agree(em, gpu, orc):
     assert rel(a["grad"], b["grad"]) <= 1e-6
 
 
+@pytest.mark.parametrize("p", [300, 1000, 3000])
+def test_checkpoint_recompute_gives_the_forward_field_bits(em, gpu, p):
+    """Within one 64-row segment both modes flush their register sums at the
+    same point, so the gradients agree bit for bit exactly when the
+    recomputed field has the forward's bits.  8192 lines x 59 rows of
+    vertices take both the four-vertex and the one-vertex passes of the
+    recompute."""
+    rng = np.random.default_rng(p)
+    n, rows = 8192, 60
+    ch = np.zeros((p, 4), np.float32)
+    ch[:, :3] = rng.uniform(-10, 10, (p, 3))
+    ch[:, 3] = rng.uniform(1, 10, p) * rng.choice([-1, 1], p, p=[0.3, 0.7])
+    d = rng.normal(size=(n, 3))
+    seeds = (d / np.linalg.norm(d, axis=1, keepdims=True)
+             * rng.uniform(35, 45, (n, 1))).astype(np.float32)
+    targets = rng.normal(0, 30, (3, rows, n)).astype(np.float32)
+    a = em.adjoint(seeds, ch, rows, targets, checkpoint=False)
+    b = em.adjoint(seeds, ch, rows, targets, checkpoint=True)
+    assert np.array_equal(a["vertices"], b["vertices"])
+    assert np.array_equal(a["grad"], b["grad"])
+
+
 def test_adjoint_repeats_bit_for_bit(em, gpu, adjoint_case):
     """Team partials are summed in a fixed order: two calls agree exactly."""
     ch, seeds, rows, targets, _ = adjoint_case
