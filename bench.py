@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
-    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "adjoint",
+    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "ext-df64", "adjoint",
                                        "adjoint-checkpoint", "adjoint-twopass",
                                        "batch", "verlet"],
                     default=None,
@@ -206,7 +206,8 @@ def run_reference(args):
 
 def run_case(args):
     """Small profiling cases (ncu captures): the extended kernel on the
-    4096-charge workload (200 rows, no termination radius), the adjoint
+    4096-charge workload (200 rows, no termination radius; FP32, mixed or
+    double-float pairs), the adjoint
     kernels on the 1024-charge workload (200 rows; stored field, or the
     field recomputed per 64-row segment; adjoint-twopass: 6000 charges, the
     two-pass backward of sets above 4096 charges), the batched tracer on the
