@@ -507,6 +507,7 @@ int em_release(void)
                     std::make_pair(&c->scratch, &c->scratch_cap),
                     std::make_pair(&c->adj, &c->adj_cap),
                     std::make_pair(&c->batch, &c->batch_cap),
+                    std::make_pair(&c->tail, &c->tail_cap),
                     std::make_pair(&c->errbuf, &c->errbuf_cap)}) {
         if (*pr.first)
             cudaFree(*pr.first);

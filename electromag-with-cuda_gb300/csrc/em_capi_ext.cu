@@ -15,7 +15,8 @@ namespace {
 
 // Layout of the per-device status block (DevCtx::errbuf, 256 B).
 constexpr size_t kOffMeta = 16, kOffQabs = 20, kOffNext = 32, kOffEvals = 40,
-                 kOffRefines = 48;
+                 kOffRefines = 48, kOffContCount = 56, kOffContNext = 64, kOffLive = 72,
+                 kOffContCount2 = 80;
 
 template <class T>
 int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl,
@@ -136,7 +137,27 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             dez = dey + elems;
         }
     }
-    cudaError_t e = cudaMemsetAsync(c.errbuf, 0, 64, s);
+    // tail hand-off for streamed charge sets (not in deterministic mode: the
+    // wide kernel sums a line's charges in another grouping): the lines left
+    // once at most half the warp slots would hold one each go to the wide
+    // kernel.  With streamed tiles every warp of a CTA waits on every tile,
+    // so a few long lines on a few warps hold whole SMs; spread over many
+    // warps they use them.  Resident sets keep the lane-group kernel, whose
+    // in-warp regrouping already serves their tails (a lone line's row takes
+    // 1.8 us there, 2.3 us in the wide kernel, whose three CTA barriers per
+    // row cost more than its wider sums save).
+    LaunchCfg wcfg = cfg;
+    wcfg.warps = 30;
+    const bool tail = !cfg.resident && !o.deterministic && !o.warps_per_cta &&
+                      cfg.smem + kExtWideSlots <= c.smem_optin;
+    const long long tail_lines = tail ? (long long)c.nsm * wcfg.warps / 2 : 0;
+    if (tail && (code = grow(&c.tail, &c.tail_cap, 2 * n * sizeof(ExtCont<T>))))
+        return code;
+    cudaError_t e = cudaMemsetAsync(c.errbuf, 0, 88, s);
+    const unsigned long long n_live = n;
+    if (e == cudaSuccess && tail)
+        e = cudaMemcpyAsync(status + kOffLive, &n_live, sizeof(n_live), cudaMemcpyHostToDevice,
+                            s);
     const cudaMemcpyKind kin = o.device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (e == cudaSuccess && p)
         e = cudaMemcpyAsync(c.charges_raw, charges, p * rec, kin, s);
@@ -186,10 +207,65 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     prm.regroup = o.deterministic ? 0 : 1;
     prm.refine_df64 = o.refine == EM_REFINE_DF64 ? 1 : 0;
     prm.err = c.err;
+    prm.cont = c.tail;
+    prm.cont_count = reinterpret_cast<unsigned long long *>(status + kOffContCount);
+    prm.cont_next = reinterpret_cast<unsigned long long *>(status + kOffContNext);
+    prm.live_count = reinterpret_cast<unsigned long long *>(status + kOffLive);
+    prm.tail_lines = tail_lines;
 
     e = cudaEventRecord(c.ev0, s);
     if (e == cudaSuccess)
         e = launch_ext_trace<T>(prm, cfg, mode, s);
+    if (e == cudaSuccess && tail) {
+        // the handed-off lines, in rounds: each round gives a line as many
+        // warps as fill the SMs, and hands its lines on to the next (wider)
+        // round once few enough are left
+        unsigned char *buf[2] = {static_cast<unsigned char *>(c.tail),
+                                 static_cast<unsigned char *>(c.tail) + n * sizeof(ExtCont<T>)};
+        unsigned long long *cnt[2] = {
+            reinterpret_cast<unsigned long long *>(status + kOffContCount),
+            reinterpret_cast<unsigned long long *>(status + kOffContCount2)};
+        const int ncw = wcfg.warps;
+        for (int round = 0; e == cudaSuccess && round < 64; ++round) {
+            const int in = round & 1, out = in ^ 1;
+            unsigned long long handed = 0;
+            e = cudaMemcpyAsync(&handed, cnt[in], sizeof(handed), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess || handed == 0)
+                break;
+            int w = 1, w_next = 0;
+            for (int d = ncw; d >= 1; --d) {
+                if (ncw % d == 0 &&
+                    (unsigned long long)c.nsm * (unsigned long long)(ncw / d) >= handed) {
+                    w = d;
+                    break;
+                }
+            }
+            for (int d = w + 1; d <= ncw; ++d) {
+                if (ncw % d == 0) {
+                    w_next = d;
+                    break;
+                }
+            }
+            const unsigned long long zero[2] = {0, 0};
+            e = cudaMemcpyAsync(cnt[out], zero, sizeof(zero[0]), cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(prm.cont_next, zero, sizeof(zero[0]),
+                                    cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(prm.live_count, &handed, sizeof(handed),
+                                    cudaMemcpyHostToDevice, s);
+            prm.cont_in = buf[in];
+            prm.cont_in_count = cnt[in];
+            prm.cont = buf[out];
+            prm.cont_count = cnt[out];
+            prm.tail_lines = w_next ? (long long)c.nsm * (ncw / w_next) : 0;
+            prm.wide = w;
+            if (e == cudaSuccess)
+                e = launch_ext_wide<T>(prm, wcfg, mode, s);
+        }
+    }
     if (e == cudaSuccess)
         e = cudaEventRecord(c.ev1, s);
     if (e == cudaSuccess && !o.device_ptrs) {

@@ -37,6 +37,8 @@ struct DevCtx {
     size_t adj_cap = 0;
     void *batch = nullptr;   // batched-tracer workspace
     size_t batch_cap = 0;
+    void *tail = nullptr;    // extended tracer: handed-off lines
+    size_t tail_cap = 0;
     int *err = nullptr;
 };
 

@@ -357,6 +357,7 @@ __global__ void __launch_bounds__(1024, 1) batch_trace_kernel(const BatchParams 
                                           : __syncthreads_or(live) != 0;
                 if (!any)
                     break;
+                const bool wlive = __any_sync(0xffffffffu, live);
                 float ax = 0, ay = 0, az = 0, dneg = 3.0e38f, dall = 3.0e38f;
                 CF hx, hy, hz;
                 st.px = px;
@@ -374,8 +375,12 @@ __global__ void __launch_bounds__(1024, 1) batch_trace_kernel(const BatchParams 
                             const int base = tile * P.tile_recs;
                             const int cnt = min(P.tile_recs, pp - base);
                             const int jn = min(max(jneg - base, 0), cnt);
-                            tile_pairs<float, EXT_FAST>(tg, tiles + sg * P.tile_recs, jn, cnt, t,
-                                                        st, ax, ay, az, dneg, dall, hx, hy, hz);
+                            // a warp with no live line only keeps the ring
+                            // turning
+                            if (wlive)
+                                tile_pairs<float, EXT_FAST>(tg, tiles + sg * P.tile_recs, jn, cnt,
+                                                            t, st, ax, ay, az, dneg, dall, hx, hy,
+                                                            hz);
                             __syncwarp();
                             if (lane == 0)
                                 mbar_arrive(empty0 + 8 * sg);

@@ -106,6 +106,96 @@ __global__ void __launch_bounds__(1024)
     }
 }
 
+// The group's field once its lanes are combined: times K, and in the
+// double-float mode the FP64 field from the two words of each sum.
+template <class T, int MODE>
+__device__ __forceinline__ void ext_field(T &ax, T &ay, T &az, const CF &hx, const CF &hy,
+                                          const CF &hz, double &Edx, double &Edy, double &Edz)
+{
+    const T K = (T)kElectroK;
+    ax = mul_rn(ax, K);
+    ay = mul_rn(ay, K);
+    az = mul_rn(az, K);
+    Edx = Edy = Edz = 0;
+    if constexpr (MODE == EXT_DF64) {
+        Edx = ((double)hx.h + (double)hx.l) * kElectroK;
+        Edy = ((double)hy.h + (double)hy.l) * kElectroK;
+        Edz = ((double)hz.h + (double)hz.l) * kElectroK;
+        ax = (T)Edx;
+        ay = (T)Edy;
+        az = (T)Edz;
+    }
+}
+
+// One vertex of a live line once its field is known: the field store, the
+// termination tests, the step (the reference rule in the mode's arithmetic,
+// curvature against the seed r0) and the vertex store; lane t == 0 of the
+// group stores.  Returns the termination class, or -1 if the line goes on
+// (s then names its next row).
+template <class T, int MODE>
+__device__ __forceinline__ int ext_vertex(const ExtParams<T> &P, long long line, int &s, int lim,
+                                          ExtLane<T> &st, int t, T ax, T ay, T az, double Edx,
+                                          double Edy, double Edz, T dneg, T r0x, T r0y, T r0z)
+{
+    const size_t n = (size_t)P.n;
+    const size_t row = (size_t)(s - 1) * n + (size_t)line;
+    if (P.ex && t == 0) {
+        P.ex[row] = ax;
+        P.ey[row] = ay;
+        P.ez[row] = az;
+    }
+    if (dneg < (T)P.term_r2)
+        return EM_TERM_CHARGE_DEV;
+    T sx, sy, sz, k2;
+    T nx, ny, nz;
+    if constexpr (MODE == EXT_DF64) {
+        // the step in FP64 from the FP64 field
+        double dsx, dsy, dsz, dk2;
+        step_vector<double>(Edx, Edy, Edz, (double)r0x, (double)r0y, (double)r0z, P.resolution,
+                            dsx, dsy, dsz, dk2);
+        k2 = (T)dk2;
+        if (dk2 > 0.0 && !(k2 > T(0)))
+            k2 = T(1); // a positive FP64 |E|^2 below the FP32 range
+        st.dx += dsx;
+        st.dy += dsy;
+        st.dz += dsz;
+        nx = (T)st.dx;
+        ny = (T)st.dy;
+        nz = (T)st.dz;
+    } else if constexpr (MODE == EXT_MIXED) {
+        step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
+        st.dx += (double)sx;
+        st.dy += (double)sy;
+        st.dz += (double)sz;
+        nx = (T)st.dx;
+        ny = (T)st.dy;
+        nz = (T)st.dz;
+    } else {
+        step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
+        nx = add_rn(st.px, sx);
+        ny = add_rn(st.py, sy);
+        nz = add_rn(st.pz, sz);
+    }
+    if (!(k2 > T(0)) || !isfinite(nx) || !isfinite(ny) || !isfinite(nz))
+        return EM_TERM_NULL_DEV;
+    st.px = nx;
+    st.py = ny;
+    st.pz = nz;
+    const size_t w = (size_t)s * n + (size_t)line;
+    if (t == 0) {
+        store_stream(P.x + w, nx);
+        store_stream(P.y + w, ny);
+        store_stream(P.z + w, nz);
+    }
+    ++s;
+    return s >= lim ? EM_TERM_STEPS_DEV : -1;
+}
+
+__device__ __forceinline__ void live_count_drop(unsigned long long *c)
+{
+    atomicAdd(c, ~0ull); // minus one
+}
+
 template <class T, int TPL, int MODE>
 __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P)
 {
@@ -136,9 +226,6 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
     __syncthreads();
     const int jneg_all = *P.meta; // padded negative block (records)
     const float qabs_max = *P.qabs; // largest |q|
-    const T K = (T)kElectroK;
-    const T term_r2 = (T)P.term_r2;
-    const size_t n = (size_t)P.n;
 
     if (!streamed) {
         if (threadIdx.x == 0) {
@@ -213,6 +300,8 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             if (t == 0) {
                 P.len[l] = 1;
                 P.cls[l] = EM_TERM_STEPS_DEV;
+                if (P.tail_lines > 0)
+                    live_count_drop(P.live_count);
             }
             return false;
         }
@@ -290,10 +379,22 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
 
     uint32_t it = 0;
     bool failed = false;
+    unsigned tail_iter = 0;
+    bool tail_check = false;
+    unsigned long long live_seen = 0;
     for (;;) {
         const bool any = streamed ? __syncthreads_or(live) != 0 : __any_sync(0xffffffffu, live);
         if (!any)
             break;
+        const bool wlive = __any_sync(0xffffffffu, live);
+        // every 8th iteration with the queue dry, lane 0 reads the number of
+        // lines still traced here (used after the pair loop, so the load's
+        // latency hides under it)
+        if (P.tail_lines > 0 && queue_empty && (++tail_iter & 7) == 0) {
+            tail_check = true;
+            if (lane == 0)
+                live_seen = *(volatile unsigned long long *)P.live_count;
+        }
         // ---- field (and nearest negative charge) at the current vertex -----
         T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
         float dall = 3.0e38f;
@@ -312,8 +413,11 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
                     const int base = tile * P.tile_recs;
                     const int jn = min(max(jneg_all - base, 0), P.tile_recs);
                     const Rec *tp = tiles + sg * P.tile_recs;
-                    tile_pairs<T, MODE>(tg, tp, jn, P.tile_recs, t, st, ax, ay, az, dneg, dall,
-                                        hx, hy, hz);
+                    // a warp with no live line only keeps the tile ring
+                    // turning (the CTA runs while any of its lines lives)
+                    if (wlive)
+                        tile_pairs<T, MODE>(tg, tp, jn, P.tile_recs, t, st, ax, ay, az, dneg,
+                                            dall, hx, hy, hz);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(empty0 + 8 * sg);
@@ -328,19 +432,8 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         }
         // ---- combine the group's lanes -------------------------------------
         combine_group<T, MODE>(tg, ax, ay, az, dneg, dall, hx, hy, hz);
-        ax = mul_rn(ax, K);
-        ay = mul_rn(ay, K);
-        az = mul_rn(az, K);
-        // double-float mode: the field in FP64 (the two words of each sum)
-        double Edx = 0, Edy = 0, Edz = 0;
-        if constexpr (MODE == EXT_DF64) {
-            Edx = ((double)hx.h + (double)hx.l) * kElectroK;
-            Edy = ((double)hy.h + (double)hy.l) * kElectroK;
-            Edz = ((double)hz.h + (double)hz.l) * kElectroK;
-            ax = (T)Edx;
-            ay = (T)Edy;
-            az = (T)Edz;
-        }
+        double Edx, Edy, Edz;
+        ext_field<T, MODE>(ax, ay, az, hx, hy, hz, Edx, Edy, Edz);
 
         if constexpr (MODE == EXT_MIXED) {
             // near a null |E| is far below its largest term and the FP32 sum
@@ -368,71 +461,42 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
                 }
             }
         }
+        // tail hand-off: with the queue dry, once few enough lines are left
+        // the warp's lines go to the wide kernel (warp-uniform decision)
+        bool hand_off = false;
+        if (tail_check) {
+            hand_off = __shfl_sync(0xffffffffu, live_seen, 0) <= (unsigned long long)P.tail_lines;
+            tail_check = false;
+        }
         if (live) {
             evals += (t == 0);
-            const size_t row = (size_t)(s - 1) * n + (size_t)line;
-            if (P.ex && t == 0) {
-                P.ex[row] = ax;
-                P.ey[row] = ay;
-                P.ez[row] = az;
-            }
-            int cls = -1;
-            if (dneg < term_r2) {
-                cls = EM_TERM_CHARGE_DEV;
-            } else {
-                const T r0x = ld_seed(P.x + line), r0y = ld_seed(P.y + line),
-                        r0z = ld_seed(P.z + line);
-                T sx, sy, sz, k2;
-                T nx, ny, nz;
-                if constexpr (MODE == EXT_DF64) {
-                    // the step in FP64 from the FP64 field
-                    double dsx, dsy, dsz, dk2;
-                    step_vector<double>(Edx, Edy, Edz, (double)r0x, (double)r0y, (double)r0z,
-                                        P.resolution, dsx, dsy, dsz, dk2);
-                    k2 = (T)dk2;
-                    if (dk2 > 0.0 && !(k2 > T(0)))
-                        k2 = T(1); // a positive FP64 |E|^2 below the FP32 range
-                    st.dx += dsx;
-                    st.dy += dsy;
-                    st.dz += dsz;
-                    nx = (T)st.dx;
-                    ny = (T)st.dy;
-                    nz = (T)st.dz;
-                } else if constexpr (MODE == EXT_MIXED) {
-                    step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
-                    st.dx += (double)sx;
-                    st.dy += (double)sy;
-                    st.dz += (double)sz;
-                    nx = (T)st.dx;
-                    ny = (T)st.dy;
-                    nz = (T)st.dz;
-                } else {
-                    step_vector<T>(ax, ay, az, r0x, r0y, r0z, (T)P.resolution, sx, sy, sz, k2);
-                    nx = add_rn(st.px, sx);
-                    ny = add_rn(st.py, sy);
-                    nz = add_rn(st.pz, sz);
-                }
-                if (!(k2 > T(0)) || !isfinite(nx) || !isfinite(ny) || !isfinite(nz)) {
-                    cls = EM_TERM_NULL_DEV;
-                } else {
-                    st.px = nx;
-                    st.py = ny;
-                    st.pz = nz;
-                    const size_t w = (size_t)s * n + (size_t)line;
-                    if (t == 0) {
-                        store_stream(P.x + w, nx);
-                        store_stream(P.y + w, ny);
-                        store_stream(P.z + w, nz);
-                    }
-                    ++s;
-                    if (s >= lim)
-                        cls = EM_TERM_STEPS_DEV;
-                }
-            }
+            const int cls = ext_vertex<T, MODE>(P, line, s, lim, st, t, ax, ay, az, Edx, Edy,
+                                                Edz, dneg, ld_seed(P.x + line),
+                                                ld_seed(P.y + line), ld_seed(P.z + line));
             if (cls >= 0) {
                 if (t == 0) {
                     P.len[line] = s;
                     P.cls[line] = cls;
+                    if (P.tail_lines > 0)
+                        live_count_drop(P.live_count);
+                }
+                live = false;
+                need = true;
+            } else if (hand_off) {
+                if (t == 0) {
+                    const unsigned long long k = atomicAdd(P.cont_count, 1ull);
+                    ExtCont<T> c;
+                    c.line = line;
+                    c.s = s;
+                    c.lim = lim;
+                    c.px = st.px;
+                    c.py = st.py;
+                    c.pz = st.pz;
+                    c.dx = st.dx;
+                    c.dy = st.dy;
+                    c.dz = st.dz;
+                    static_cast<ExtCont<T> *>(P.cont)[k] = c;
+                    live_count_drop(P.live_count);
                 }
                 live = false;
                 need = true;
@@ -451,6 +515,388 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         if (refines)
             atomicAdd(P.refines, refines);
     }
+}
+
+// ---------------------------------------------------------------------------
+// The handed-off lines, W = P.wide warps per line (a group); the groups of a
+// CTA step in lockstep, three CTA barriers per row.  Warp w of a group sums
+// the charges of its W-th of each tile (or of the resident set) with all 32
+// lanes; the warps' sums meet in shared memory, the group's first warp (its
+// lead) combines them, runs the vertex step and publishes the new vertex,
+// which the other warps read after the row's last barrier.  A group whose
+// line ends takes the next handed-off line.
+template <class T, int MODE>
+__global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
+{
+    using Rec = typename ChargeRec<T>::type;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ T slots[32][8];       // each warp's sums (T words, no conversions)
+    __shared__ double rslots[32][4]; // each warp's re-evaluation sums
+    __shared__ long long grp_next[32];
+    __shared__ T grp_pos[32][3];     // the lead's vertex after the step
+    __shared__ int grp_flag[32];     // 1: the line goes on; 2: re-evaluate
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    Rec *tiles = reinterpret_cast<Rec *>(smem + 128);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const bool streamed = !P.resident;
+    const int ncw = streamed ? nwarps - 1 : nwarps;
+    const int NST = streamed ? P.stages : 1;
+    const int W = P.wide;
+    if (NST > 8 || ncw < 1 || ncw > 32 || W < 1 || ncw % W != 0) {
+        if (threadIdx.x == 0)
+            atomicCAS(P.err, 0, EM_DEVERR_CONFIG);
+        return;
+    }
+    const uint32_t full0 = smem_addr(bars), empty0 = smem_addr(bars + 8);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NST; ++k) {
+            mbar_init(full0 + 8 * k, 1);
+            mbar_init(empty0 + 8 * k, ncw);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int jneg_all = *P.meta;
+    const float qabs_max = *P.qabs;
+    const long long count = (long long)*P.cont_in_count;
+    const ExtCont<T> *cont = static_cast<const ExtCont<T> *>(P.cont_in);
+    __shared__ unsigned long long sh_live;
+
+    if (!streamed) {
+        if (threadIdx.x == 0) {
+            const uint32_t bytes = (uint32_t)P.p_pad * (uint32_t)sizeof(Rec);
+            mbar_arrive_expect_tx(full0, bytes);
+            const char *src = static_cast<const char *>(P.charges);
+            const uint32_t dst = smem_addr(tiles);
+            constexpr uint32_t CH = 32768;
+            for (uint32_t off = 0; off < bytes; off += CH)
+                bulk_g2s(dst + off, src + off, bytes - off < CH ? bytes - off : CH, full0);
+        }
+        // every thread passes the CTA barriers below, so none may leave here
+        mbar_wait(full0, 0, P.err);
+    }
+
+    if (streamed && warp == nwarps - 1) {
+        // ---- producer: the tiles of every row while any group has a line;
+        // it passes the consumers' CTA barriers in the same order
+        __syncthreads(); // first lines taken
+        const uint32_t tb = (uint32_t)P.tile_recs * (uint32_t)sizeof(Rec);
+        const char *src = static_cast<const char *>(P.charges);
+        uint32_t it = 0;
+        bool ok = true;
+        while (__syncthreads_or(0)) {
+            if (lane == 0 && ok && *(volatile int *)P.err == 0) {
+                for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+                    const uint32_t sg = it % NST, ph = (it / NST) & 1;
+                    if (it >= (uint32_t)NST && !mbar_wait(empty0 + 8 * sg, ph ^ 1, P.err)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(full0 + 8 * sg, tb);
+                    bulk_g2s(smem_addr(tiles) + sg * tb, src + (size_t)tile * tb, tb,
+                             full0 + 8 * sg);
+                }
+            }
+            __syncwarp();
+            __syncthreads_or(0); // the warps' sums are in the slots
+            if constexpr (MODE == EXT_MIXED) {
+                if (__syncthreads_or(0))
+                    __syncthreads(); // re-evaluation sums
+            }
+            __syncthreads(); // next lines taken
+        }
+        if (lane == 0) {
+            for (uint32_t k = 0; k < (uint32_t)NST && k < it; ++k) {
+                const uint32_t j = it - 1 - k;
+                mbar_wait(full0 + 8 * (j % NST), (j / NST) & 1, P.err);
+            }
+        }
+        return;
+    }
+
+    // ---- consumers --------------------------------------------------------
+    const int g = warp / W, wg = warp - g * W;
+    const bool lead = wg == 0;
+    const int t = wg * 32 + lane; // thread index within the group
+    long long line = -1;
+    int s = 1, lim = 0;
+    bool live = false;
+    ExtLane<T> st;
+    st.px = st.py = st.pz = 0;
+    st.dx = st.dy = st.dz = 0;
+    unsigned long long evals = 0, refines = 0;
+    auto take = [&]() {
+        const long long k = grp_next[g];
+        if (k < count) {
+            const ExtCont<T> c = cont[k];
+            line = c.line;
+            s = c.s;
+            lim = c.lim;
+            st.px = c.px;
+            st.py = c.py;
+            st.pz = c.pz;
+            st.dx = c.dx;
+            st.dy = c.dy;
+            st.dz = c.dz;
+            live = true;
+        } else {
+            line = -1;
+            live = false;
+        }
+    };
+    auto save = [&]() {
+        const unsigned long long k = atomicAdd(P.cont_count, 1ull);
+        ExtCont<T> c;
+        c.line = line;
+        c.s = s;
+        c.lim = lim;
+        c.px = st.px;
+        c.py = st.py;
+        c.pz = st.pz;
+        c.dx = st.dx;
+        c.dy = st.dy;
+        c.dz = st.dz;
+        static_cast<ExtCont<T> *>(P.cont)[k] = c;
+    };
+    if (lead && lane == 0)
+        grp_next[g] = (long long)atomicAdd(P.cont_next, 1ull);
+    __syncthreads(); // first lines taken
+    take();
+
+    uint32_t it = 0;
+    bool failed = false;
+    unsigned row_iter = 0;
+    for (;;) {
+        if (!__syncthreads_or(live))
+            break;
+        // every 8th row: are few enough lines left to hand them on to a
+        // wider launch?  (read here, used after the next barrier)
+        const bool tail_check = P.tail_lines > 0 && (++row_iter & 7) == 0;
+        if (tail_check && threadIdx.x == 0)
+            sh_live = *(volatile unsigned long long *)P.live_count;
+        // the seed (the lead's curvature reference), read while the pairs run
+        T r0x = 0, r0y = 0, r0z = 0;
+        if (lead && live) {
+            r0x = ld_seed(P.x + line);
+            r0y = ld_seed(P.y + line);
+            r0z = ld_seed(P.z + line);
+        }
+        T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
+        float dall = 3.0e38f;
+        CF hx, hy, hz;
+        if (!streamed) {
+            const int b = (int)((long long)P.p_pad * wg / W);
+            const int e = (int)((long long)P.p_pad * (wg + 1) / W);
+            const int jn = min(max(jneg_all - b, 0), e - b);
+            if (live)
+                tile_pairs<T, MODE>(32, tiles + b, jn, e - b, lane, st, ax, ay, az, dneg, dall,
+                                    hx, hy, hz);
+        } else {
+            const int b = (int)((long long)P.tile_recs * wg / W);
+            const int e = (int)((long long)P.tile_recs * (wg + 1) / W);
+            for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+                const uint32_t sg = it % NST, ph = (it / NST) & 1;
+                if (!failed && !mbar_wait(full0 + 8 * sg, ph, P.err))
+                    failed = true;
+                if (!failed) {
+                    const int base = tile * P.tile_recs;
+                    const int jt = min(max(jneg_all - base, 0), P.tile_recs);
+                    const int jn = min(max(jt - b, 0), e - b);
+                    if (live)
+                        tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane, st,
+                                            ax, ay, az, dneg, dall, hx, hy, hz);
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(empty0 + 8 * sg);
+                }
+            }
+        }
+        // ---- each warp's sums into the slots -------------------------------
+        if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+            group_two_sum<32>(hx);
+            group_two_sum<32>(hy);
+            group_two_sum<32>(hz);
+            dall = group_min<float, 32>(dall);
+        } else {
+            ax = group_sum<T, 32>(ax);
+            ay = group_sum<T, 32>(ay);
+            az = group_sum<T, 32>(az);
+        }
+        dneg = group_min<T, 32>(dneg);
+        if (lane == 0) {
+            T *o = slots[warp];
+            if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+                o[0] = hx.h;
+                o[1] = hx.l;
+                o[2] = hy.h;
+                o[3] = hy.l;
+                o[4] = hz.h;
+                o[5] = hz.l;
+            } else {
+                o[0] = ax;
+                o[1] = ay;
+                o[2] = az;
+            }
+            o[6] = dneg;
+            o[7] = (T)dall;
+        }
+        // a wait that gave up in any warp stops every group (CTA-uniform)
+        if (__syncthreads_or(failed)) {
+            live = false;
+            failed = true;
+        }
+        const bool hand_off = tail_check && sh_live <= (unsigned long long)P.tail_lines;
+        // ---- the lead combines the group's sums (lane w takes warp w's) ----
+        double Edx = 0, Edy = 0, Edz = 0;
+        bool redo = false;
+        if (lead) {
+            const T *gs = slots[g * W + (lane < W ? lane : 0)];
+            const bool mine = lane < W;
+            if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+                hx.h = mine ? gs[0] : 0.0f;
+                hx.l = mine ? gs[1] : 0.0f;
+                hy.h = mine ? gs[2] : 0.0f;
+                hy.l = mine ? gs[3] : 0.0f;
+                hz.h = mine ? gs[4] : 0.0f;
+                hz.l = mine ? gs[5] : 0.0f;
+                group_two_sum<32>(hx);
+                group_two_sum<32>(hy);
+                group_two_sum<32>(hz);
+                ax = (T)__fadd_rn(hx.h, hx.l);
+                ay = (T)__fadd_rn(hy.h, hy.l);
+                az = (T)__fadd_rn(hz.h, hz.l);
+                dall = group_min<float, 32>(mine ? (float)gs[7] : 3.0e38f);
+            } else {
+                ax = group_sum<T, 32>(mine ? gs[0] : T(0));
+                ay = group_sum<T, 32>(mine ? gs[1] : T(0));
+                az = group_sum<T, 32>(mine ? gs[2] : T(0));
+            }
+            dneg = group_min<T, 32>(mine ? gs[6] : T(3.0e38));
+            ext_field<T, MODE>(ax, ay, az, hx, hy, hz, Edx, Edy, Edz);
+            if constexpr (MODE == EXT_MIXED) {
+                const float bound = qabs_max * (float)kElectroK / dall;
+                const float e2 = ax * ax + ay * ay + az * az;
+                const float lim2 = (float)P.null_frac * bound;
+                redo = live && !(e2 >= lim2 * lim2);
+                if (lane == 0)
+                    grp_flag[g] = redo ? 2 : 0;
+            }
+        }
+        if constexpr (MODE == EXT_MIXED) {
+            // near a null: the group re-evaluates the field in FP64 (or
+            // double-float), each warp its W-th of the staged records
+            if (__syncthreads_or(redo)) {
+                const bool gredo = grp_flag[g] == 2;
+                double fx = 0, fy = 0, fz = 0;
+                if (gredo) {
+                    const int cb = (int)((long long)P.p_pad * wg / W);
+                    const int ce = (int)((long long)P.p_pad * (wg + 1) / W);
+                    const float4 *cr = reinterpret_cast<const float4 *>(P.charges) + cb;
+                    if (P.refine_df64)
+                        field_df64<32>(cr, ce - cb, lane, (float)st.px, (float)st.py,
+                                       (float)st.pz, fx, fy, fz);
+                    else
+                        field_fp64<32>(cr, ce - cb, lane, (double)(float)st.px,
+                                       (double)(float)st.py, (double)(float)st.pz, fx, fy, fz);
+                    fx = group_sum<double, 32>(fx);
+                    fy = group_sum<double, 32>(fy);
+                    fz = group_sum<double, 32>(fz);
+                    if (lane == 0) {
+                        rslots[warp][0] = fx;
+                        rslots[warp][1] = fy;
+                        rslots[warp][2] = fz;
+                    }
+                }
+                __syncthreads();
+                if (lead && redo) {
+                    const double *gs = rslots[g * W + (lane < W ? lane : 0)];
+                    const bool mine = lane < W;
+                    fx = group_sum<double, 32>(mine ? gs[0] : 0.0);
+                    fy = group_sum<double, 32>(mine ? gs[1] : 0.0);
+                    fz = group_sum<double, 32>(mine ? gs[2] : 0.0);
+                    ax = (T)(fx * kElectroK);
+                    ay = (T)(fy * kElectroK);
+                    az = (T)(fz * kElectroK);
+                    refines += (lane == 0);
+                }
+            }
+        }
+        // ---- the lead's vertex step ----------------------------------------
+        bool need = false;
+        if (lead && live) {
+            evals += (lane == 0);
+            const int cls = ext_vertex<T, MODE>(P, line, s, lim, st, t, ax, ay, az, Edx, Edy,
+                                                Edz, dneg, r0x, r0y, r0z);
+            int flag = 1;
+            if (cls >= 0) {
+                if (lane == 0) {
+                    P.len[line] = s;
+                    P.cls[line] = cls;
+                    if (P.tail_lines > 0)
+                        live_count_drop(P.live_count);
+                    grp_next[g] = (long long)atomicAdd(P.cont_next, 1ull);
+                }
+                flag = 0;
+                need = true;
+            } else if (hand_off) {
+                // every input line was taken at the start (a group each),
+                // so nothing is left behind
+                if (lane == 0) {
+                    save();
+                    live_count_drop(P.live_count);
+                }
+                flag = 0;
+            }
+            if (lane == 0) {
+                grp_flag[g] = flag | (need ? 4 : 0);
+                grp_pos[g][0] = st.px;
+                grp_pos[g][1] = st.py;
+                grp_pos[g][2] = st.pz;
+            }
+        }
+        __syncthreads(); // the leads' vertices and next lines are out
+        if (live && !failed) {
+            const int flag = grp_flag[g];
+            if (flag & 4) {
+                take();
+            } else if (flag & 1) {
+                if (!lead) {
+                    st.px = grp_pos[g][0];
+                    st.py = grp_pos[g][1];
+                    st.pz = grp_pos[g][2];
+                }
+            } else {
+                live = false;
+            }
+        }
+    }
+    // counters: one atomic per warp
+    for (int o = 16; o; o >>= 1) {
+        evals += __shfl_xor_sync(0xffffffffu, evals, o);
+        refines += __shfl_xor_sync(0xffffffffu, refines, o);
+    }
+    if (lane == 0) {
+        atomicAdd(P.evals, evals);
+        if (refines)
+            atomicAdd(P.refines, refines);
+    }
+}
+
+template <class T, int MODE>
+cudaError_t launch_ext_wide_mode(const ExtParams<T> &p, const LaunchCfg &cfg,
+                                 cudaStream_t stream)
+{
+    auto kern = ext_wide_kernel<T, MODE>;
+    cudaError_t e =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess)
+        return e;
+    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
+    kern<<<cfg.grid, threads, cfg.smem, stream>>>(p);
+    count_launch(1);
+    return cudaGetLastError();
 }
 
 template <class T, int TPL, int MODE>
@@ -509,6 +955,25 @@ cudaError_t launch_ext_trace<double>(const ExtParams<double> &p, const LaunchCfg
     if (mode != EXT_FAST)
         return cudaErrorInvalidValue;
     return launch_ext_mode<double, EXT_FAST>(p, cfg, stream);
+}
+
+template <>
+cudaError_t launch_ext_wide<float>(const ExtParams<float> &p, const LaunchCfg &cfg, int mode,
+                                   cudaStream_t stream)
+{
+    if (mode == EXT_DF64)
+        return launch_ext_wide_mode<float, EXT_DF64>(p, cfg, stream);
+    return mode == EXT_MIXED ? launch_ext_wide_mode<float, EXT_MIXED>(p, cfg, stream)
+                             : launch_ext_wide_mode<float, EXT_FAST>(p, cfg, stream);
+}
+
+template <>
+cudaError_t launch_ext_wide<double>(const ExtParams<double> &p, const LaunchCfg &cfg, int mode,
+                                    cudaStream_t stream)
+{
+    if (mode != EXT_FAST)
+        return cudaErrorInvalidValue;
+    return launch_ext_wide_mode<double, EXT_FAST>(p, cfg, stream);
 }
 
 template cudaError_t launch_ext_stage<float>(const void *, int, void *, int, int, int *, float *,

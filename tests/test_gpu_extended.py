@@ -179,6 +179,49 @@ def test_regrouping_tail_agrees_and_is_faster(em, gpu, orc):
     assert b["perf"].time < a["perf"].time
 
 
+@pytest.mark.parametrize("precision", ["fp32", "mixed", "df64", "fp64"])
+def test_streamed_tail_handoff_matches_fp64_oracle(em, gpu, ext_case, precision):
+    """Streamed tiles (64 charges each): once the queue is dry and few lines
+    are left, they go to the wide kernel (several warps per line, in rounds
+    that widen as lines finish).  Classes and vertices still meet the
+    oracle criteria, and every evaluated vertex is counted once."""
+    ch, seeds, steps, ref = ext_case
+    c = ch.astype(np.float64) if precision == "fp64" else ch
+    out = em.trace_lines(seeds, c, steps, 1.0, 0.5, precision=precision,
+                         force_streamed=True, tile_charges=64)
+    agree, vok, gl, gc = compare(out, ref)
+    assert agree >= CLASS_AGREE, agree
+    assert vok >= CLASS_AGREE, vok
+    assert np.all((gl >= 1) & (gl <= steps))
+    assert out["perf"].pairs == pytest.approx(
+        float(np.sum(gl - 1 + (gc != 0))) * len(ch), rel=0, abs=0)
+
+
+def test_streamed_tail_handoff_long_lines(em, gpu):
+    """A few long lines among many short ones on a streamed set: the long
+    lines finish in the wide kernel with the lengths of the deterministic
+    (lane-group only) run and vertices within tolerance of it, faster."""
+    ch, seeds, _ = em.workloads.make("cpu_256", seed=5)
+    seeds = seeds.astype(np.float32)
+    lim = np.full(len(seeds), 30, np.int32)
+    lim[::97] = 3000
+    kw = dict(steps_per_line=lim, force_streamed=True, tile_charges=64)
+    a = em.trace_lines(seeds, ch, 3000, 1.0, 0.0, deterministic=True, **kw)
+    b = em.trace_lines(seeds, ch, 3000, 1.0, 0.0, **kw)
+    assert np.array_equal(a["len"], b["len"])
+    assert np.array_equal(a["cls"], b["cls"])
+    with np.errstate(invalid="ignore", over="ignore"):
+        # rows at and after a line's length are unspecified
+        A = a["vertices"].astype(np.float64)
+        B = b["vertices"].astype(np.float64)
+    for i in np.nonzero(lim == 3000)[0]:
+        m = min(a["len"][i], 200)
+        err = np.abs(A[:, :m, i] - B[:, :m, i]) / np.maximum(np.abs(A[:, :m, i]), 1)
+        assert err.max() <= VERTEX_RTOL
+    assert a["perf"].pairs == b["perf"].pairs
+    assert b["perf"].time < a["perf"].time
+
+
 def _fields_at_vertices(out, step=4):
     V, F, gl = out["vertices"], out["field"], out["len"]
     pts, fld = [], []
