@@ -400,13 +400,19 @@ def main():
 
 def metric_parts(value, extras):
     """The metric's parts in one place: the plain FP32 rate (`value`), the
-    mixed-precision tracer against it per pair (200 rows, no termination)
-    with its field error vs FP64, and the adjoint/forward time ratio."""
+    mixed-precision tracer per pair (200 rows, no termination) against it
+    and against the extended tracer's own FP32 form (the same lane-group
+    kernel, the per-pair cost of the mixed arithmetic alone), its field
+    error vs FP64, and the adjoint/forward time ratio."""
     parts = {"plain_fp32_gpair_s": value}
     prec = extras.get("precision", {})
     if "mixed_vs_fp32" in prec:
         mixed = prec.get("mixed", {}).get("field_err_vs_fp64") or {}
-        parts.update({"mixed_vs_plain_fp32": prec["mixed_vs_fp32"],
+        rates = prec.get("no_termination_200_rows_gpair_s", {})
+        parts.update({"mixed_gpair_s": rates.get("mixed"),
+                      "mixed_vs_plain_fp32": (rates["mixed"] / value
+                                              if rates.get("mixed") else None),
+                      "mixed_vs_extended_fp32": prec["mixed_vs_fp32"],
                       "mixed_vs_fp64": prec.get("mixed_vs_fp64"),
                       "mixed_field_err_median": mixed.get("median"),
                       "mixed_field_err_max": mixed.get("max"),
