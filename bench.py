@@ -400,10 +400,12 @@ def main():
 
 def metric_parts(value, extras):
     """The metric's parts in one place: the plain FP32 rate (`value`), the
-    mixed-precision tracer per pair (200 rows, no termination) against it
-    and against the extended tracer's own FP32 form (the same lane-group
+    extended tracer's mixed mode per pair (200 rows, no termination) against
+    it and against the extended tracer's own FP32 form (the same lane-group
     kernel, the per-pair cost of the mixed arithmetic alone), its field
-    error vs FP64, and the adjoint/forward time ratio."""
+    error vs FP64, the mixed arithmetic on the reference-layout tracer (the
+    same loop as `value`) against `value`, and the adjoint/forward time
+    ratio."""
     parts = {"plain_fp32_gpair_s": value}
     prec = extras.get("precision", {})
     if "mixed_vs_fp32" in prec:
@@ -417,6 +419,10 @@ def metric_parts(value, extras):
                       "mixed_field_err_median": mixed.get("median"),
                       "mixed_field_err_max": mixed.get("max"),
                       "mixed_frac_le_1e-6": mixed.get("frac_le_1e-6")})
+    mref = extras.get("mixed_reference_layout", {})
+    if "gpair_s" in mref:
+        parts["mixed_reference_layout_gpair_s"] = mref["gpair_s"]
+        parts["mixed_reference_layout_vs_plain_fp32"] = mref["gpair_s"] / value
     adj = extras.get("adjoint", {})
     if "stored" in adj:
         parts["adjoint_over_forward"] = adj["stored"]["adjoint_over_forward"]
@@ -730,6 +736,31 @@ def nbody_functor_block(em, torch, dev, seed):
     return blk
 
 
+def mixed_reference_block(em, torch, dev, args):
+    """The mixed arithmetic on the reference-layout tracer (EM_ARITH_MIXED):
+    the `value` workload and loop (every line all rows, device arrays), so
+    its rate divides by `value` directly."""
+    ch, seeds, rows = workload(em, args.workload, args.seed + 0, args.rows)
+    n, p = len(seeds), len(ch)
+    X = [torch.zeros(n * rows, dtype=torch.float32, device=dev) for _ in range(3)]
+    for c in range(3):
+        X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c])).to(dev)
+    dch = torch.from_numpy(ch).to(dev)
+    times = []
+    for i in range(3):
+        rc, perf = em.calc_field(*X, dch, n, 1.0, True, require_n64=False,
+                                 arith="mixed")
+        if rc:
+            raise em.EmError(rc, "em_calc_field_ex_f32 (mixed)")
+        if i:
+            times.append(perf.time)
+    torch.cuda.synchronize()
+    t = float(np.mean(times))
+    pairs = float(n) * (rows - 1) * p
+    return {"workload": args.workload, "lines": n, "charges": p, "rows": rows,
+            "ms": t * 1e3, "gpair_s": pairs / t / 1e9}
+
+
 def run_extras(em, torch, dev, args):
     """Single-GPU measurements of the other configurations; a block that
     fails is reported in its place and does not cost the bench line."""
@@ -738,6 +769,7 @@ def run_extras(em, torch, dev, args):
         ("batched", lambda: batch_block(em, torch, dev, args.seed)),
         ("precision", lambda: precision_block(em, torch, dev, args.workload,
                                               5000, args.seed, 20000, True)),
+        ("mixed_reference_layout", lambda: mixed_reference_block(em, torch, dev, args)),
         ("precision_stress", lambda: precision_block(
             em, torch, dev, "dipole_16384", 4000, args.seed, 20000, False)),
         ("adjoint", lambda: adjoint_block(em, torch, dev, args.seed)),

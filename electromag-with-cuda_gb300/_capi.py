@@ -32,6 +32,7 @@ EM_ERR_TOO_LARGE = 14
 EM_NOALLOC_MAX_CHARGES = 16384
 EM_ARITH_FAST = 0
 EM_ARITH_EXACT = 1
+EM_ARITH_MIXED = 2
 EM_PACK_AUTO = 0
 EM_PACK_SCALAR = 1
 EM_PACK_PAIRS = 2

@@ -133,9 +133,12 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     em_options o{};
     if (opt)
         o = *opt;
-    if (o.arith != EM_ARITH_FAST && o.arith != EM_ARITH_EXACT)
+    if (o.arith != EM_ARITH_FAST && o.arith != EM_ARITH_EXACT &&
+        !(o.arith == EM_ARITH_MIXED && sizeof(T) == 4))
         return EM_ERR_ARG;
     if (o.rule != EM_RULE_SSE && o.rule != EM_RULE_GENERIC)
+        return EM_ERR_ARG;
+    if (!(o.null_frac >= 0))
         return EM_ERR_ARG;
     if (total_steps > (size_t)INT_MAX || p > (size_t)(INT_MAX / 64) ||
         n > (size_t)(LLONG_MAX / 64) / total_steps)
@@ -188,7 +191,11 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         e = launch_stage_charges<T>(c.charges_raw, (int)p, c.charges, pl.p_pad,
                                     stage_layout(pl.arith), pl.cfg.tile_recs, s);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(c.err, 0, sizeof(int), s);
+        e = cudaMemsetAsync(c.errbuf, 0, 64, s);
+    // mixed: the largest |q| bounds a single contribution (status word 20)
+    float *qabs = reinterpret_cast<float *>(static_cast<unsigned char *>(c.errbuf) + 20);
+    if (e == cudaSuccess && pl.arith == ARITH_MIXED && p)
+        e = launch_abs_charge_max(static_cast<const float *>(c.charges_raw), (int)p, qabs, s);
     if (e == cudaSuccess && !o.device_ptrs) {
         e = cudaMemcpyAsync(dx, x + line0, nl * sizeof(T), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
@@ -215,13 +222,16 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     prm.rule = use_curvature ? o.rule : RULE_FIXED;
     prm.resolution = resolution;
     prm.err = c.err;
+    prm.qabs = qabs;
+    prm.null_frac = o.null_frac > 0 ? o.null_frac : 1e-4;
 
     // Host arrays, all lines: trace in row chunks and copy each finished
     // chunk to the host on the copy stream while the next one is traced
     // (rows are contiguous blocks of n values; a chunk resumes from the last
-    // row of the one before, so the result is the one-launch result).
+    // row of the one before, so the result is the one-launch result; not in
+    // the mixed form, whose FP64 position a stored FP32 row would round).
     const bool chunked = !o.device_ptrs && nl == n && elems * sizeof(T) * 3 >= (64u << 20) &&
-                         total_steps >= 64;
+                         total_steps >= 64 && pl.arith != ARITH_MIXED;
     const int nchunks = chunked ? 8 : 1;
     e = cudaEventRecord(c.ev0, s);
     for (int k = 0; k < nchunks && e == cudaSuccess; ++k) {

@@ -26,6 +26,7 @@ enum Arith : int {
     ARITH_FAST = 0,  // rsqrt + FMA, k applied once per vertex
     ARITH_EXACT = 1, // the reference's IEEE operation sequence, bit-exact
     ARITH_FAST2 = 2, // fast form on packed FP32 pairs (.f32x2), paired charge layout
+    ARITH_MIXED = 3, // FP32 pairs + corrected inv^3 + compensation, FP64 position
 };
 
 // Charge record: pointCharge<T> of include/Electrostatics.h:30-35.
@@ -61,6 +62,9 @@ template <class T> struct RefTraceParams {
     // the seeds the SSE rule's curvature reads (null: row 0 of x, y, z); a
     // launch that resumes a trace passes x, y, z from its start row
     const T *seed_x, *seed_y, *seed_z;
+    // mixed arithmetic: largest |q| and the re-evaluation threshold
+    const float *qabs;
+    double null_frac;
 };
 
 // Extended tracer (em_trace_ext.cu).
@@ -245,6 +249,8 @@ constexpr int kUnroll = 8;
 template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream);
+// Largest |q| of p raw records (FP32 bits, a non-negative float) into *out.
+cudaError_t launch_abs_charge_max(const float *raw, int p, float *out, cudaStream_t stream);
 
 // Stages p raw charge records into p_pad records (pad record {1e15, 1e15,
 // 1e15, 0}, whose contribution is exactly zero), plain (paired = 0) or in

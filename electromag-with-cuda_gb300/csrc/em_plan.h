@@ -131,7 +131,11 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
         return EM_ERR_ARG;
     if (o.pack < EM_PACK_AUTO || o.pack > EM_PACK_PAIRS)
         return EM_ERR_ARG;
-    int arith = o.arith == EM_ARITH_EXACT ? ARITH_EXACT : ARITH_FAST;
+    if (o.arith == EM_ARITH_MIXED && sizeof(T) != 4)
+        return EM_ERR_ARG;
+    int arith = o.arith == EM_ARITH_EXACT   ? ARITH_EXACT
+                : o.arith == EM_ARITH_MIXED ? ARITH_MIXED
+                                            : ARITH_FAST;
     // packed pairs only on request: each .f32x2 FMA holds the FMA pipe for
     // two cycles, so it saves issue slots but not pipe time
     if (arith == ARITH_FAST && sizeof(T) == 4 && o.pack == EM_PACK_PAIRS)
@@ -141,9 +145,14 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     // lines per lane: searched for the fast scalar form when the caller does
     // not say (two lines share each charge load, one line doubles the warps
     // for small line counts); 2 for packed pairs, 1 for exact arithmetic
+    // (mixed: 1 unless asked; two lines' compensated sums and FP64
+    // positions do not fit the 80 registers of a 768-thread CTA: 1536
+    // against 1732 Gpair/s on 32 736 lines x 4096 charges)
     int fixed_kl = 1;
     if (arith == ARITH_FAST)
         fixed_kl = o.lines_per_thread;
+    else if (arith == ARITH_MIXED)
+        fixed_kl = o.lines_per_thread ? o.lines_per_thread : 1;
     else if (arith == ARITH_FAST2)
         fixed_kl = o.lines_per_thread ? o.lines_per_thread : 2;
     const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
@@ -152,10 +161,13 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     const size_t gran_max = 16 * kUnroll;
     const size_t p_res = (p + gran_max - 1) / gran_max * gran_max;
     const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
-    choose_shape((long long)n, (long long)p, c.nsm, resident ? 32 : 31, fixed_tpl, fixed_kl,
-                 &tpl, &kl, &warps);
+    // the mixed form's per-line sums need more than 64 registers: at most
+    // 768 threads (80 registers) per CTA
+    const int max_warps = (arith == ARITH_MIXED ? 24 : 32) - (resident ? 0 : 1);
+    choose_shape((long long)n, (long long)p, c.nsm, max_warps, fixed_tpl, fixed_kl, &tpl, &kl,
+                 &warps);
     if (o.warps_per_cta)
-        warps = std::min(o.warps_per_cta, resident ? 32 : 31);
+        warps = std::min(o.warps_per_cta, max_warps);
     // records per padding granule: every lane gets whole unrolled groups
     const int gran = tpl * kUnroll * (arith == ARITH_FAST2 ? 2 : 1);
     Plan r;

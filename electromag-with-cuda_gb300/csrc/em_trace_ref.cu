@@ -20,6 +20,7 @@
 // per-vertex step (curvature, vec3SetInvLen, include/Vector.h:157-164) uses
 // the IEEE sequence in both modes.
 #include "em_device.cuh"
+#include "em_ext.cuh"
 #include "em_internal.h"
 #include "em_math.cuh"
 
@@ -150,6 +151,48 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
     }
 }
 
+// Mixed arithmetic (FP32 records only): the pairs of records [0, count) of
+// KL lines for lane t of TPL, the inv^3 Newton correction, compensated
+// every kChunk pairs per lane into each line's (hi, lo) sums; dall gets the
+// nearest distance^2 (the null test's contribution bound).
+template <int TPL, int KL>
+__device__ __forceinline__ void accumulate_mixed(const float4 *tile, int count, int t,
+                                                 const float *px, const float *py,
+                                                 const float *pz, CF *hx, CF *hy, CF *hz,
+                                                 float *dall)
+{
+    for (int j0 = t; j0 < count; j0 += TPL * kChunk) {
+        const int j1 = min(count, j0 + TPL * kChunk);
+        float ax[KL], ay[KL], az[KL];
+#pragma unroll
+        for (int k = 0; k < KL; ++k)
+            ax[k] = ay[k] = az[k] = 0.0f;
+#pragma unroll 4
+        for (int j = j0; j < j1; j += TPL) {
+            const float4 c = tile[j];
+#pragma unroll
+            for (int k = 0; k < KL; ++k) {
+                const float dx = px[k] - c.x, dy = py[k] - c.y, dz = pz[k] - c.z;
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                dall[k] = fminf(dall[k], r2);
+                const float inv = rsqrt_fast(r2);
+                const float inv2 = inv * inv;
+                const float s0 = (c.w * inv) * inv2;
+                const float sc = s0 * fmaf(-1.5f * r2, inv2, 2.5f);
+                ax[k] = fmaf(sc, dx, ax[k]);
+                ay[k] = fmaf(sc, dy, ay[k]);
+                az[k] = fmaf(sc, dz, az[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < KL; ++k) {
+            hx[k].add(ax[k]);
+            hy[k].add(ay[k]);
+            hz[k].add(az[k]);
+        }
+    }
+}
+
 template <class T, int TPL, int ARITH, int KL, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams<T> P)
 {
@@ -244,6 +287,7 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
         long long line[KL];
         bool own[KL];
         T px[KL], py[KL], pz[KL];
+        double qx[KL], qy[KL], qz[KL]; // mixed: the FP64 position
 #pragma unroll
         for (int k = 0; k < KL; ++k) {
             // slot k of the warp's lines: consecutive lanes -> consecutive lines
@@ -255,20 +299,37 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                 py[k] = P.y[line[k]];
                 pz[k] = P.z[line[k]];
             }
+            qx[k] = (double)px[k];
+            qy[k] = (double)py[k];
+            qz[k] = (double)pz[k];
         }
         for (int step = 1; step < P.total_steps; ++step) {
             Acc<T> acc[KL];
+            CF hx[KL], hy[KL], hz[KL];
+            float dall[KL];
+#pragma unroll
+            for (int k = 0; k < KL; ++k)
+                dall[k] = 3.0e38f;
+            auto charges_of = [&](const Rec *tp, int count) {
+                if constexpr (ARITH == ARITH_MIXED)
+                    accumulate_mixed<TPL, KL>(reinterpret_cast<const float4 *>(tp), count, t,
+                                              reinterpret_cast<const float *>(px),
+                                              reinterpret_cast<const float *>(py),
+                                              reinterpret_cast<const float *>(pz), hx, hy, hz,
+                                              dall);
+                else
+                    accumulate_k<T, TPL, ARITH, KL>(tp, count, t, px, py, pz, K, three_arg,
+                                                    acc);
+            };
             if (!streamed) {
-                accumulate_k<T, TPL, ARITH, KL>(tiles, P.p_pad, t, px, py, pz, K, three_arg,
-                                                acc);
+                charges_of(tiles, P.p_pad);
             } else {
                 for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
                     const uint32_t s = it % NST, ph = (it / NST) & 1;
                     if (!mbar_wait(full0 + 8 * s, ph, P.err))
                         return;
                     if (active)
-                        accumulate_k<T, TPL, ARITH, KL>(tiles + s * P.tile_recs, P.tile_recs, t,
-                                                        px, py, pz, K, three_arg, acc);
+                        charges_of(tiles + s * P.tile_recs, P.tile_recs);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(empty0 + 8 * s);
@@ -280,7 +341,14 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
             for (int k = 0; k < KL; ++k) {
                 acc_finish<T, ARITH>(acc[k]);
                 T ax = acc[k].x, ay = acc[k].y, az = acc[k].z;
-                if (TPL > 1) {
+                if constexpr (ARITH == ARITH_MIXED) {
+                    group_two_sum<TPL>(hx[k]);
+                    group_two_sum<TPL>(hy[k]);
+                    group_two_sum<TPL>(hz[k]);
+                    ax = (T)__fadd_rn(hx[k].h, hx[k].l);
+                    ay = (T)__fadd_rn(hy[k].h, hy[k].l);
+                    az = (T)__fadd_rn(hz[k].h, hz[k].l);
+                } else if (TPL > 1) {
                     ax = line_reduce<T, TPL>(ax);
                     ay = line_reduce<T, TPL>(ay);
                     az = line_reduce<T, TPL>(az);
@@ -307,8 +375,42 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                     r0y = ld_seed(P.seed_y + line[k]);
                     r0z = ld_seed(P.seed_z + line[k]);
                 }
-                advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k], py[k],
-                           pz[k]);
+                if constexpr (ARITH == ARITH_MIXED) {
+                    // near a null |E| is far below its largest term and the
+                    // FP32 sum loses its digits: the field again in FP64
+                    const float dmin = group_min<float, TPL>(dall[k]);
+                    const float bound = *P.qabs * (float)kElectroK / dmin;
+                    const float e2 = (float)(ax * ax + ay * ay + az * az);
+                    const float lim2 = (float)P.null_frac * bound;
+                    const bool redo = own[k] && !(e2 >= lim2 * lim2);
+                    if (__any_sync(0xffffffffu, redo)) {
+                        double fx = 0, fy = 0, fz = 0;
+                        if (redo)
+                            field_fp64<TPL>(static_cast<const float4 *>(P.charges), P.p_pad, t,
+                                            (double)px[k], (double)py[k], (double)pz[k], fx,
+                                            fy, fz);
+                        fx = group_sum<double, TPL>(fx);
+                        fy = group_sum<double, TPL>(fy);
+                        fz = group_sum<double, TPL>(fz);
+                        if (redo) {
+                            ax = (T)(fx * kElectroK);
+                            ay = (T)(fy * kElectroK);
+                            az = (T)(fz * kElectroK);
+                        }
+                    }
+                    // the reference's step in FP32, the position in FP64
+                    T sx, sy, sz;
+                    step_of<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, sx, sy, sz);
+                    qx[k] += (double)sx;
+                    qy[k] += (double)sy;
+                    qz[k] += (double)sz;
+                    px[k] = (T)qx[k];
+                    py[k] = (T)qy[k];
+                    pz[k] = (T)qz[k];
+                } else {
+                    advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k],
+                               py[k], pz[k]);
+                }
                 if (own[k] && t == 0) {
                     const size_t idx = (size_t)step * n + (size_t)line[k];
                     store_stream(P.x + idx, px[k]);
@@ -385,6 +487,17 @@ cudaError_t launch_fast(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaSt
 }
 
 template <class T, int TPL>
+cudaError_t launch_mixed(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
+{
+    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
+    if (cfg.kl == 2)
+        return threads <= 768 ? launch_one<T, TPL, ARITH_MIXED, 2, 768>(p, cfg, stream)
+                              : launch_one<T, TPL, ARITH_MIXED, 2, 1024>(p, cfg, stream);
+    return threads <= 768 ? launch_one<T, TPL, ARITH_MIXED, 1, 768>(p, cfg, stream)
+                          : launch_one<T, TPL, ARITH_MIXED, 1, 1024>(p, cfg, stream);
+}
+
+template <class T, int TPL>
 cudaError_t launch_packed(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
 {
     return cfg.kl == 2 ? launch_one<T, TPL, ARITH_FAST2, 2, 1024>(p, cfg, stream)
@@ -409,6 +522,19 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &params, const LaunchCfg &c
         if (cfg.tpl != 1)
             return cudaErrorInvalidValue;
         return launch_one<T, 1, ARITH_EXACT, 1, 1024>(p, cfg, stream);
+    }
+    if (arith == ARITH_MIXED) {
+        if constexpr (sizeof(T) != 4) {
+            return cudaErrorInvalidValue;
+        } else {
+            switch (cfg.tpl) {
+            case 1: return launch_mixed<T, 1>(p, cfg, stream);
+            case 2: return launch_mixed<T, 2>(p, cfg, stream);
+            case 4: return launch_mixed<T, 4>(p, cfg, stream);
+            case 8: return launch_mixed<T, 8>(p, cfg, stream);
+            default: return cudaErrorInvalidValue;
+            }
+        }
     }
     if (arith == ARITH_FAST2) {
         if (sizeof(T) != 4)
@@ -440,6 +566,38 @@ cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad
         return cudaErrorInvalidValue;
     stage_kernel<T><<<(p_pad + 127) / 128, 128, 0, stream>>>(
         static_cast<const T *>(raw), p, static_cast<T *>(staged), p_pad, paired, block);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+namespace {
+
+// Largest |q| over p records, one CTA of 256 (a warp maximum per warp, then
+// the CTA's).
+__global__ void __launch_bounds__(256) abs_charge_max_kernel(const float *raw, int p, float *out)
+{
+    __shared__ float wm[8];
+    float m = 0;
+    for (int i = threadIdx.x; i < p; i += blockDim.x)
+        m = fmaxf(m, fabsf(raw[4 * (size_t)i + 3]));
+    for (int o = 16; o; o >>= 1)
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0)
+        wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            r = fmaxf(r, wm[w]);
+        *out = r;
+    }
+}
+
+} // namespace
+
+cudaError_t launch_abs_charge_max(const float *raw, int p, float *out, cudaStream_t stream)
+{
+    abs_charge_max_kernel<<<1, 256, 0, stream>>>(raw, p, out);
     count_launch(1);
     return cudaGetLastError();
 }

@@ -15,7 +15,8 @@ import numpy as np
 
 from . import _capi
 
-_ARITH = {"fast": _capi.EM_ARITH_FAST, "exact": _capi.EM_ARITH_EXACT}
+_ARITH = {"fast": _capi.EM_ARITH_FAST, "exact": _capi.EM_ARITH_EXACT,
+          "mixed": _capi.EM_ARITH_MIXED}
 _RULE = {"sse": _capi.EM_RULE_SSE, "generic": _capi.EM_RULE_GENERIC}
 _PACK = {"auto": _capi.EM_PACK_AUTO, "scalar": _capi.EM_PACK_SCALAR,
          "pairs": _capi.EM_PACK_PAIRS}
@@ -48,8 +49,13 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                arith="fast", rule="sse", require_n64=None, stream=None,
                threads_per_line=0, warps_per_cta=0, tile_charges=0,
                force_streamed=False, pack="auto", lines_per_thread=0,
-               plain=None):
+               plain=None, null_frac=0.0):
     """Traces n field lines in place; returns (rc, perf).
+
+    arith: "fast" (FP32/FP64 rsqrt + FMA), "exact" (the reference's IEEE
+    sequence) or "mixed" (float32 only: compensated FP32 pairs with a
+    Newton-corrected inv^3, the position in FP64, the field re-evaluated in
+    FP64 below null_frac (default 1e-4) of the largest contribution).
 
     rc is the reference's code (0 ok, 1 n == 0, 2 resolution == 0,
     3 total_steps < 2, 5 n % 64 with require_n64) or a library code >= 4.
@@ -67,7 +73,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     device = _is_torch(x) and x.is_cuda
     perf = _capi.EmPerf()
     if plain is None:
-        plain = (not device and arith == "fast" and rule == "sse"
+        plain = (not device and arith == "fast" and rule == "sse" and not null_frac
                  and require_n64 in (None, True) and not threads_per_line
                  and not warps_per_cta and not tile_charges
                  and not force_streamed and pack == "auto"
@@ -95,6 +101,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     o.force_streamed = int(bool(force_streamed))
     o.pack = _PACK[pack]
     o.lines_per_thread = lines_per_thread
+    o.null_frac = null_frac
     fn = lib.em_calc_field_ex_f32 if f32 else lib.em_calc_field_ex_f64
     rc = fn(_ptr(x), _ptr(y), _ptr(z), n, total_steps, _ptr(charges), p,
             resolution, int(bool(use_curvature)), ctypes_byref(o),

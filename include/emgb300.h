@@ -58,6 +58,12 @@ extern "C" {
 #define EM_ARITH_FAST 0   /* FP32 (or FP64 for _f64) rsqrt + FMA             */
 #define EM_ARITH_EXACT 1  /* the reference's IEEE operation sequence:
                              bit-identical to its strict x86 build          */
+#define EM_ARITH_MIXED 2  /* _f32 only: FP32 pairs with a Newton-corrected
+                             inv^3, compensated sums, the line position in
+                             FP64, the field re-evaluated in FP64 where |E|
+                             is below null_frac of the largest single
+                             contribution (the extended tracer's
+                             EM_PREC_MIXED, on the reference's loop)        */
 
 /* ---- stepping rule (which reference routine to reproduce) ---------------- */
 #define EM_RULE_SSE 0      /* CalcField_CPU_T_Curvature<float/double> SSE
