@@ -137,18 +137,20 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             dez = dey + elems;
         }
     }
-    // tail hand-off for streamed charge sets (not in deterministic mode: the
-    // wide kernel sums a line's charges in another grouping): the lines left
-    // once at most half the warp slots would hold one each go to the wide
-    // kernel.  With streamed tiles every warp of a CTA waits on every tile,
-    // so a few long lines on a few warps hold whole SMs; spread over many
-    // warps they use them.  Resident sets keep the lane-group kernel, whose
-    // in-warp regrouping already serves their tails (a lone line's row takes
+    // tail hand-off (not in deterministic mode: the wide kernel sums a
+    // line's charges in another grouping): the lines left once at most half
+    // the warp slots would hold one each go to the wide kernel.  With
+    // streamed tiles every warp of a CTA waits on every tile, so a few long
+    // lines on a few warps hold whole SMs; spread over many warps they use
+    // them.  With resident charges the lane-group kernel's in-warp
+    // regrouping serves the FP32 forms' tails (a lone FP32 line's row takes
     // 1.8 us there, 2.3 us in the wide kernel, whose three CTA barriers per
-    // row cost more than its wider sums save).
+    // row cost more than its wider sums save); the double-float and FP64
+    // pairs cost 10-60x more, so their lone lines gain from more warps.
     LaunchCfg wcfg = cfg;
-    wcfg.warps = 30;
-    const bool tail = !cfg.resident && !o.deterministic && !o.warps_per_cta &&
+    wcfg.warps = cfg.resident ? 32 : 30;
+    const bool heavy = mode == EXT_DF64 || sizeof(T) == 8;
+    const bool tail = (!cfg.resident || heavy) && !o.deterministic && !o.warps_per_cta &&
                       cfg.smem + kExtWideSlots <= c.smem_optin;
     const long long tail_lines = tail ? (long long)c.nsm * wcfg.warps / 2 : 0;
     if (tail && (code = grow(&c.tail, &c.tail_cap, 2 * n * sizeof(ExtCont<T>))))
@@ -226,6 +228,15 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             reinterpret_cast<unsigned long long *>(status + kOffContCount),
             reinterpret_cast<unsigned long long *>(status + kOffContCount2)};
         const int ncw = wcfg.warps;
+        // with resident charges a warp's share of a row must outweigh the
+        // two warp reductions and the barriers per row: at least 12
+        // double-float pairs per lane (about 150 instructions each), 2 FP64
+        // ones (1/64 rate); streamed rows also wait on the tile ring, so
+        // there the count alone sets W
+        int w_cap = ncw;
+        if (cfg.resident)
+            w_cap = (int)std::max<long long>(
+                1, std::min<long long>(ncw, p_pad / (32LL * (sizeof(T) == 8 ? 2 : 12))));
         for (int round = 0; e == cudaSuccess && round < 64; ++round) {
             const int in = round & 1, out = in ^ 1;
             unsigned long long handed = 0;
@@ -235,14 +246,14 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             if (e != cudaSuccess || handed == 0)
                 break;
             int w = 1, w_next = 0;
-            for (int d = ncw; d >= 1; --d) {
+            for (int d = w_cap; d >= 1; --d) {
                 if (ncw % d == 0 &&
                     (unsigned long long)c.nsm * (unsigned long long)(ncw / d) >= handed) {
                     w = d;
                     break;
                 }
             }
-            for (int d = w + 1; d <= ncw; ++d) {
+            for (int d = w + 1; d <= w_cap; ++d) {
                 if (ncw % d == 0) {
                     w_next = d;
                     break;

@@ -381,19 +381,24 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
     bool failed = false;
     unsigned tail_iter = 0;
     bool tail_check = false;
-    unsigned long long live_seen = 0;
+    unsigned long long live_seen = 0, next_seen = 0;
     for (;;) {
         const bool any = streamed ? __syncthreads_or(live) != 0 : __any_sync(0xffffffffu, live);
         if (!any)
             break;
         const bool wlive = __any_sync(0xffffffffu, live);
-        // every 8th iteration with the queue dry, lane 0 reads the number of
-        // lines still traced here (used after the pair loop, so the load's
-        // latency hides under it)
-        if (P.tail_lines > 0 && queue_empty && (++tail_iter & 7) == 0) {
+        // every 8th iteration lane 0 reads the queue head (a warp whose lines
+        // all run long would otherwise learn that the queue is dry only when
+        // one of them ends) and, with the hand-off, the number of lines still
+        // traced here; used after the pair loop, so the loads' latency hides
+        // under it
+        if ((++tail_iter & 7) == 0 && (!queue_empty || P.tail_lines > 0)) {
             tail_check = true;
-            if (lane == 0)
-                live_seen = *(volatile unsigned long long *)P.live_count;
+            if (lane == 0) {
+                next_seen = *(volatile unsigned long long *)P.next_line;
+                if (P.tail_lines > 0)
+                    live_seen = *(volatile unsigned long long *)P.live_count;
+            }
         }
         // ---- field (and nearest negative charge) at the current vertex -----
         T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
@@ -465,7 +470,12 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         // the warp's lines go to the wide kernel (warp-uniform decision)
         bool hand_off = false;
         if (tail_check) {
-            hand_off = __shfl_sync(0xffffffffu, live_seen, 0) <= (unsigned long long)P.tail_lines;
+            const unsigned long long ns = __shfl_sync(0xffffffffu, next_seen, 0);
+            if ((long long)ns + total_slots >= P.n)
+                queue_empty = true;
+            if (P.tail_lines > 0)
+                hand_off = queue_empty && __shfl_sync(0xffffffffu, live_seen, 0) <=
+                                              (unsigned long long)P.tail_lines;
             tail_check = false;
         }
         if (live) {
