@@ -96,6 +96,11 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
         if (128 + (size_t)cfg.stages * tile * rec > smem_cap)
             return EM_ERR_ARG;
         n_tiles = (int)ceil_div(p_min, tile);
+        if (!o.tile_charges) {
+            // the same number of tiles, evened out: no nearly empty last
+            // tile of pad records (p = 16384 would pay 6 % more pairs)
+            tile = (int)(ceil_div(ceil_div(p_min, n_tiles), gran) * gran);
+        }
         p_pad = n_tiles * tile;
         cfg.warps = o.warps_per_cta ? std::min(o.warps_per_cta, 31) : 31;
         cfg.smem = 128 + (size_t)cfg.stages * tile * rec;
@@ -149,9 +154,27 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     // pairs cost 10-60x more, so their lone lines gain from more warps.
     LaunchCfg wcfg = cfg;
     wcfg.warps = cfg.resident ? 32 : 30;
+    int wide_tiles = n_tiles;
+    if (!cfg.resident) {
+        // streamed: a wide group splits every tile W ways, so its warps
+        // take the staged tiles up to four at a time (the last one
+        // shorter), in as many stages (2..4) as fit beside the static slots:
+        // fewer waits and loop set-ups per pair
+        const size_t room = smem_cap > kExtWideSlots + 128 ? smem_cap - kExtWideSlots - 128 : 0;
+        for (int m = 4; m >= 1; m >>= 1) {
+            const size_t tb = (size_t)tile * m * rec;
+            if (2 * tb <= room) {
+                wcfg.tile_recs = tile * m;
+                wcfg.stages = (int)std::min<size_t>(4, room / tb);
+                wcfg.smem = 128 + (size_t)wcfg.stages * tb;
+                wide_tiles = (int)ceil_div(n_tiles, m);
+                break;
+            }
+        }
+    }
     const bool heavy = mode == EXT_DF64 || sizeof(T) == 8;
     const bool tail = (!cfg.resident || heavy) && !o.deterministic && !o.warps_per_cta &&
-                      cfg.smem + kExtWideSlots <= c.smem_optin;
+                      wcfg.smem + kExtWideSlots <= c.smem_optin;
     const long long tail_lines = tail ? (long long)c.nsm * wcfg.warps / 2 : 0;
     if (tail && (code = grow(&c.tail, &c.tail_cap, 2 * n * sizeof(ExtCont<T>))))
         return code;
@@ -273,8 +296,12 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             prm.cont_count = cnt[out];
             prm.tail_lines = w_next ? (long long)c.nsm * (ncw / w_next) : 0;
             prm.wide = w;
+            ExtParams<T> wp = prm;
+            wp.n_tiles = wide_tiles;
+            wp.tile_recs = wcfg.tile_recs;
+            wp.stages = wcfg.stages;
             if (e == cudaSuccess)
-                e = launch_ext_wide<T>(prm, wcfg, mode, s);
+                e = launch_ext_wide<T>(wp, wcfg, mode, s);
         }
     }
     if (e == cudaSuccess)

@@ -46,6 +46,13 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
+// Arrives on the pending phase and leaves: later phases expect one arrival
+// fewer (a consumer that will read no further tiles).
+__device__ __forceinline__ void mbar_arrive_drop(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive_drop.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),

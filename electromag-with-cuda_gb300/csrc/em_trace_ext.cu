@@ -381,12 +381,23 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
     bool failed = false;
     unsigned tail_iter = 0;
     bool tail_check = false;
+    bool in_ring = true; // streamed: still consuming the tile ring
     unsigned long long live_seen = 0, next_seen = 0;
     for (;;) {
         const bool any = streamed ? __syncthreads_or(live) != 0 : __any_sync(0xffffffffu, live);
         if (!any)
             break;
         const bool wlive = __any_sync(0xffffffffu, live);
+        if (streamed && in_ring && !wlive && queue_empty) {
+            // no line now and none to come: leave the tile ring (every tile
+            // of the rows so far is consumed; the producer's later waits
+            // count one consumer fewer) instead of waiting on every tile
+            __syncwarp();
+            if (lane == 0)
+                for (int k = 0; k < NST; ++k)
+                    mbar_arrive_drop(empty0 + 8 * k);
+            in_ring = false;
+        }
         // every 8th iteration lane 0 reads the queue head (a warp whose lines
         // all run long would otherwise learn that the queue is dry only when
         // one of them ends) and, with the hand-off, the number of lines still
@@ -408,7 +419,7 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             tile_pairs<T, MODE>(tg, tiles, jneg_all, P.p_pad, t, st, ax, ay, az, dneg, dall, hx,
                                 hy, hz);
         } else {
-            for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+            for (int tile = 0; in_ring && tile < P.n_tiles; ++tile, ++it) {
                 const uint32_t sg = it % NST, ph = (it / NST) & 1;
                 // on a failed wait the warp stops computing but keeps voting,
                 // so the CTA-wide loop still ends for every thread
@@ -604,8 +615,13 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
                         ok = false;
                         break;
                     }
-                    mbar_arrive_expect_tx(full0 + 8 * sg, tb);
-                    bulk_g2s(smem_addr(tiles) + sg * tb, src + (size_t)tile * tb, tb,
+                    // the last tile may be shorter (tiles of several staged
+                    // tiles; p_pad is a multiple of the staged tile)
+                    const uint32_t bytes =
+                        (uint32_t)min(P.tile_recs, P.p_pad - tile * P.tile_recs) *
+                        (uint32_t)sizeof(Rec);
+                    mbar_arrive_expect_tx(full0 + 8 * sg, bytes);
+                    bulk_g2s(smem_addr(tiles) + sg * tb, src + (size_t)tile * tb, bytes,
                              full0 + 8 * sg);
                 }
             }
@@ -677,10 +693,19 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
 
     uint32_t it = 0;
     bool failed = false;
+    bool in_ring = true; // streamed: still consuming the tile ring
     unsigned row_iter = 0;
     for (;;) {
         if (!__syncthreads_or(live))
             break;
+        if (streamed && in_ring && !live) {
+            // a group without a line now has none to come: its warps leave
+            // the tile ring (all tiles of earlier rows are consumed)
+            if (lane == 0)
+                for (int k = 0; k < NST; ++k)
+                    mbar_arrive_drop(empty0 + 8 * k);
+            in_ring = false;
+        }
         // every 8th row: are few enough lines left to hand them on to a
         // wider launch?  (read here, used after the next barrier)
         const bool tail_check = P.tail_lines > 0 && (++row_iter & 7) == 0;
@@ -704,15 +729,16 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
                 tile_pairs<T, MODE>(32, tiles + b, jn, e - b, lane, st, ax, ay, az, dneg, dall,
                                     hx, hy, hz);
         } else {
-            const int b = (int)((long long)P.tile_recs * wg / W);
-            const int e = (int)((long long)P.tile_recs * (wg + 1) / W);
-            for (int tile = 0; tile < P.n_tiles; ++tile, ++it) {
+            for (int tile = 0; in_ring && tile < P.n_tiles; ++tile, ++it) {
                 const uint32_t sg = it % NST, ph = (it / NST) & 1;
                 if (!failed && !mbar_wait(full0 + 8 * sg, ph, P.err))
                     failed = true;
                 if (!failed) {
                     const int base = tile * P.tile_recs;
-                    const int jt = min(max(jneg_all - base, 0), P.tile_recs);
+                    const int recs = min(P.tile_recs, P.p_pad - base);
+                    const int b = (int)((long long)recs * wg / W);
+                    const int e = (int)((long long)recs * (wg + 1) / W);
+                    const int jt = min(max(jneg_all - base, 0), recs);
                     const int jn = min(max(jt - b, 0), e - b);
                     if (live)
                         tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane, st,
