@@ -147,11 +147,8 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     // the warp slots would hold one each go to the wide kernel.  With
     // streamed tiles every warp of a CTA waits on every tile, so a few long
     // lines on a few warps hold whole SMs; spread over many warps they use
-    // them.  With resident charges the lane-group kernel's in-warp
-    // regrouping serves the FP32 forms' tails (a lone FP32 line's row takes
-    // 1.8 us there, 2.3 us in the wide kernel, whose three CTA barriers per
-    // row cost more than its wider sums save); the double-float and FP64
-    // pairs cost 10-60x more, so their lone lines gain from more warps.
+    // them.  With resident charges a lone line gains from more warps as
+    // long as each warp keeps enough pairs per row (w_cap below).
     LaunchCfg wcfg = cfg;
     wcfg.warps = cfg.resident ? 32 : 30;
     int wide_tiles = n_tiles;
@@ -172,8 +169,22 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             }
         }
     }
-    const bool heavy = mode == EXT_DF64 || sizeof(T) == 8;
-    const bool tail = (!cfg.resident || heavy) && !o.deterministic && !o.warps_per_cta &&
+    // with resident charges a warp's share of a row must outweigh the two
+    // warp reductions and the barriers per row: at least 32 FP32 pairs per
+    // lane (about 14 instructions each), 24 mixed, 12 double-float (about
+    // 150), 2 FP64 (1/64 rate); below two warps per line the lane-group
+    // kernel's regrouping (a warp per line) serves the tail better.
+    // Streamed rows also wait on the tile ring, so there the count alone
+    // sets W.
+    int w_cap = wcfg.warps;
+    if (cfg.resident) {
+        const long long per_lane = sizeof(T) == 8       ? 2
+                                   : mode == EXT_DF64  ? 12
+                                   : mode == EXT_MIXED ? 24
+                                                       : 32;
+        w_cap = (int)std::min<long long>(wcfg.warps, p_pad / (32LL * per_lane));
+    }
+    const bool tail = !o.deterministic && !o.warps_per_cta && w_cap >= 2 &&
                       wcfg.smem + kExtWideSlots <= c.smem_optin;
     const long long tail_lines = tail ? (long long)c.nsm * wcfg.warps / 2 : 0;
     if (tail && (code = grow(&c.tail, &c.tail_cap, 2 * n * sizeof(ExtCont<T>))))
@@ -251,15 +262,6 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             reinterpret_cast<unsigned long long *>(status + kOffContCount),
             reinterpret_cast<unsigned long long *>(status + kOffContCount2)};
         const int ncw = wcfg.warps;
-        // with resident charges a warp's share of a row must outweigh the
-        // two warp reductions and the barriers per row: at least 12
-        // double-float pairs per lane (about 150 instructions each), 2 FP64
-        // ones (1/64 rate); streamed rows also wait on the tile ring, so
-        // there the count alone sets W
-        int w_cap = ncw;
-        if (cfg.resident)
-            w_cap = (int)std::max<long long>(
-                1, std::min<long long>(ncw, p_pad / (32LL * (sizeof(T) == 8 ? 2 : 12))));
         for (int round = 0; e == cudaSuccess && round < 64; ++round) {
             const int in = round & 1, out = in ^ 1;
             unsigned long long handed = 0;
