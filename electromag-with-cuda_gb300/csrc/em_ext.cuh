@@ -183,14 +183,6 @@ __device__ __forceinline__ DF df_fast(float a, float b)
     return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 
-__device__ __forceinline__ DF df_sqr(DF a)
-{
-    const float p = __fmul_rn(a.h, a.h);
-    float e = __fmaf_rn(a.h, a.h, -p);
-    e = __fmaf_rn(__fadd_rn(a.h, a.h), a.l, e);
-    return df_fast(p, e);
-}
-
 __device__ __forceinline__ DF df_mul(DF a, DF b)
 {
     const float p = __fmul_rn(a.h, b.h);
@@ -208,31 +200,58 @@ __device__ __forceinline__ DF df_mul_f(DF a, float b)
     return df_fast(p, e);
 }
 
-__device__ __forceinline__ DF df_add(DF a, DF b)
+// Square of a double-float as an unnormalised pair: the product of the
+// high words exactly (FMA), the cross term folded into the low word (the
+// low word squared, below 2^-48 of the result, is dropped).
+__device__ __forceinline__ void df_sqr_parts(DF a, float &p, float &e)
 {
-    const DF s = df_two_sum(a.h, b.h);
-    return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+    p = __fmul_rn(a.h, a.h);
+    e = __fmaf_rn(a.h, a.h, -p);
+    e = __fmaf_rn(__fadd_rn(a.h, a.h), a.l, e);
+}
+
+// a * b for double-float a and b as an unnormalised pair (the caller's
+// compensated accumulator takes the two words separately)
+__device__ __forceinline__ DF df_mul_raw(DF a, DF b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return {p, e};
 }
 
 // q r / |r|^3 for the FP32 point p and charge c, each component a DF; r2h
 // gets |r|^2 rounded to FP32 (for the nearest-negative test).
+//   r = p - c exactly (two-sums); |r|^2 from the three exact squares, the
+//   high words summed by two-sums and the low words added plainly (about
+//   2^-46 relative); y0 = rsqrt(|r|^2) in FP32 and eps = 1 - |r|^2 y0^2 in
+//   double-float, so |r|^-3 = y0^3 (1 - eps)^(-3/2) = y0^3 (1 + 1.5 eps)
+//   to within 15/8 eps^2 (|eps| < 2^-21: about 2^-42 relative).
 __device__ __forceinline__ void df_pair(float px, float py, float pz, const float4 &c, DF &tx,
                                         DF &ty, DF &tz, float &r2h)
 {
     const DF dx = df_two_sum(px, -c.x), dy = df_two_sum(py, -c.y), dz = df_two_sum(pz, -c.z);
-    const DF r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+    float sx, ex, sy, ey, sz, ez;
+    df_sqr_parts(dx, sx, ex);
+    df_sqr_parts(dy, sy, ey);
+    df_sqr_parts(dz, sz, ez);
+    const DF s1 = df_two_sum(sx, sy);
+    const DF s2 = df_two_sum(s1.h, sz);
+    const DF r2 = df_fast(s2.h, __fadd_rn(__fadd_rn(__fadd_rn(ex, ey), ez),
+                                          __fadd_rn(s1.l, s2.l)));
     r2h = r2.h;
-    // r^-1/2: the FP32 estimate, then one Newton step on the double-float
-    // residual h = 1 - r2 y0^2 (1 - t.h is exact: t.h is within 2^-21 of 1)
     const float y0 = rsqrt_fast(r2.h);
-    const DF y2 = {__fmul_rn(y0, y0), __fmaf_rn(y0, y0, -__fmul_rn(y0, y0))};
-    const DF t = df_mul(r2, y2);
-    const float hres = __fsub_rn(__fsub_rn(1.0f, t.h), t.l);
-    const DF inv = df_fast(y0, __fmul_rn(__fmul_rn(y0, 0.5f), hres));
-    const DF s = df_mul_f(df_mul(df_sqr(inv), inv), c.w);
-    tx = df_mul(s, dx);
-    ty = df_mul(s, dy);
-    tz = df_mul(s, dz);
+    const float y2h = __fmul_rn(y0, y0);
+    const DF y2 = {y2h, __fmaf_rn(y0, y0, -y2h)};
+    const DF t = df_mul(r2, y2);                              // 1 - eps
+    const float eps = __fsub_rn(__fsub_rn(1.0f, t.h), t.l);   // t.h is within 2^-21 of 1
+    const DF y3 = df_mul_f(y2, y0);                           // y0^3
+    const DF s = df_fast(y3.h, __fmaf_rn(y3.h, __fmul_rn(1.5f, eps), y3.l));
+    const DF qs = df_mul_f(s, c.w);
+    tx = df_mul_raw(qs, dx);
+    ty = df_mul_raw(qs, dy);
+    tz = df_mul_raw(qs, dz);
 }
 
 // The compensated accumulator takes a double-float term: its high word with
