@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
-    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "ext-df64", "adjoint",
+    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "ext-df64",
+                                       "ext-tail-dipole", "adjoint",
                                        "adjoint-checkpoint", "adjoint-twopass",
                                        "batch", "verlet"],
                     default=None,
@@ -207,7 +208,8 @@ def run_reference(args):
 def run_case(args):
     """Small profiling cases (ncu captures): the extended kernel on the
     4096-charge workload (200 rows, no termination radius; FP32, mixed or
-    double-float pairs), the adjoint
+    double-float pairs), the extended tracer with its tail kernel on the
+    dipole set (1000 rows, termination radius 0.5), the adjoint
     kernels on the 1024-charge workload (200 rows; stored field, or the
     field recomputed per 64-row segment; adjoint-twopass: 6000 charges, the
     two-pass backward of sets above 4096 charges), the batched tracer on the
@@ -229,6 +231,14 @@ def run_case(args):
         torch.cuda.synchronize()
         perf = out["perf"]
         print("batch", perf.pairs / perf.time / 1e9, "Gpair/s")
+        return 0
+    if args.case == "ext-tail-dipole":
+        ch, seeds, _ = em.workloads.make("dipole_16384", seed=args.seed)
+        ch = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).to(dev)
+        s = torch.from_numpy(seeds.astype(np.float32)).to(dev)
+        out = em.trace_lines(s, ch, 1000, 1.0, 0.5)
+        torch.cuda.synchronize()
+        print("tail", out["perf"].pairs / out["perf"].time / 1e9, "Gpair/s")
         return 0
     if args.case.startswith("ext"):
         ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)
