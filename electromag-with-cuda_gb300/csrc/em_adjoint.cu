@@ -780,7 +780,7 @@ cudaError_t launch_fused(const AdjParams &P, const AdjFused &f, int lo, int hi,
 
 cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, int nsm,
                                     size_t smem, double *loss, double *grad,
-                                    cudaStream_t stream)
+                                    cudaStream_t stream, cudaStream_t side, size_t half_elems)
 {
     cudaError_t e = cudaFuncSetAttribute(adj_line_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -811,15 +811,47 @@ cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, i
             if ((e = launch_fused(P, *fused, 0, P.rows - 1, stream)) != cudaSuccess)
                 return e;
         } else {
-            for (int hi = P.rows - 1; hi > 0; hi -= seg) {
-                const int lo = std::max(0, hi - seg);
+            // the recompute of the next segment overlaps the fused kernel of
+            // this one (each fills the SMs the other's last CTAs leave);
+            // buffer half k % 2, reused once the fused kernel of segment
+            // k - 2 has read it
+            cudaEvent_t ev[5] = {};
+            for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+                e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+            cudaEvent_t *field_done = ev, *fused_done = ev + 2, start = ev[4];
+            if (e == cudaSuccess)
+                e = cudaEventRecord(start, stream); // forward, loss and init are in
+            if (e == cudaSuccess)
+                e = cudaStreamWaitEvent(side, start, 0);
+            int k = 0;
+            for (int hi = P.rows - 1; hi > 0 && e == cudaSuccess; hi -= seg, ++k) {
+                const int lo = std::max(0, hi - seg), h = k & 1;
                 AdjParams Q = P;
                 Q.f_row0 = lo;
-                adj_field_kernel<<<field_grid, kFieldThreads, smem, stream>>>(Q, lo, hi);
+                Q.fx = P.fx + h * half_elems;
+                Q.fy = P.fy + h * half_elems;
+                Q.fz = P.fz + h * half_elems;
+                if (k >= 2)
+                    e = cudaStreamWaitEvent(side, fused_done[h], 0);
+                if (e != cudaSuccess)
+                    break;
+                adj_field_kernel<<<field_grid, kFieldThreads, smem, side>>>(Q, lo, hi);
                 count_launch(1);
-                if ((e = launch_fused(Q, *fused, lo, hi, stream)) != cudaSuccess)
-                    return e;
+                e = cudaGetLastError();
+                if (e == cudaSuccess)
+                    e = cudaEventRecord(field_done[h], side);
+                if (e == cudaSuccess)
+                    e = cudaStreamWaitEvent(stream, field_done[h], 0);
+                if (e == cudaSuccess)
+                    e = launch_fused(Q, *fused, lo, hi, stream);
+                if (e == cudaSuccess)
+                    e = cudaEventRecord(fused_done[h], stream);
             }
+            for (int j = 0; j < 5; ++j)
+                if (ev[j])
+                    cudaEventDestroy(ev[j]);
+            if (e != cudaSuccess)
+                return e;
         }
         const dim3 sgrid((unsigned)((P.p + 255) / 256), (unsigned)P.slices);
         adj_team_sum_kernel<<<sgrid, 256, 0, stream>>>(P);

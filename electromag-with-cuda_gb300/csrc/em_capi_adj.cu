@@ -79,11 +79,11 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
             1, std::min<long long>(std::max(1, 4 * c.nsm / cb), (recs + 2047) / 2048));
     }
     // adjoint workspace: abar (3n f32); records (6 * seg * n f32, two-pass)
-    // or the field (3 * rows * n f32 stored, 3 * seg * n f32 recomputed) and
+    // or the field (3 * rows * n f32 stored, 3 * 2 seg * n f32 recomputed) and
     // the team partials (teams * 4 * p_bwd float2, fused); slice partials
     // (slices * p * 4 f64); the loss and its per-CTA partials, then grad (4p f64)
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t field_rows = stored ? rows : (size_t)kSeg;
+    const size_t field_rows = stored ? rows : 2 * (size_t)kSeg; // two halves when recomputed
     const size_t off_rec = up(3 * n * 4);
     const size_t rec_bytes = fused ? 3 * field_rows * n * 4 : 6 * (size_t)recs * 4;
     const size_t off_tpart = off_rec + up(rec_bytes);
@@ -201,7 +201,8 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
         e = cudaEventRecord(c.ev1, s);
     if (e == cudaSuccess)
         e = launch_adjoint_backward(ap, fused ? &af : nullptr, c.nsm,
-                                    128 + (size_t)pl.p_pad * 16, dloss, dgrad, s);
+                                    128 + (size_t)pl.p_pad * 16, dloss, dgrad, s, c.copy_stream,
+                                    (size_t)kSeg * n);
     if (e == cudaSuccess)
         e = cudaEventRecord(ev2, s);
     if (e == cudaSuccess)

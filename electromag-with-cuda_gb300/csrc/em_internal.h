@@ -177,9 +177,13 @@ int adjoint_loss_parts(int nsm);
 int adjoint_fused_plan(int p, int nsm, AdjFused *f);
 // fused == nullptr: the two-pass backward (field recompute + Jacobian-vector
 // kernel, then the charge-stationary kernel) per 64-row segment.
+// Checkpoint mode (fused, field not stored): the field of segment k is
+// recomputed on `side` into half k % 2 of a two-segment buffer (half_elems
+// apart) while the fused kernel of segment k - 1 runs on `stream`.
 cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, int nsm,
                                     size_t smem, double *loss, double *grad,
-                                    cudaStream_t stream);
+                                    cudaStream_t stream, cudaStream_t side,
+                                    size_t half_elems);
 
 // Batched tracing (em_trace_batch.cu).
 struct BatchParams {
