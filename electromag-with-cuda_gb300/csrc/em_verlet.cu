@@ -65,28 +65,46 @@ template <class T> struct VerletArgs {
     T dt;
 };
 
+// Particles per thread: each source record read from shared memory feeds
+// kParts pairs (one per particle the thread holds), a quarter of the shared
+// loads per pair of one particle per thread (the first form, shared-memory
+// bound at 982 Gpair/s; two particles 1154, four 1279 on 65 536 moving and
+// 4096 static charges).  Each particle's sums run in the same order as with
+// one particle per thread, so the bits do not depend on kParts.
+constexpr int kParts = 4;
+constexpr int kTile = 512; // records per shared-memory tile
+
+// Pairs of the moving sources tile[0, count) with the kParts particles of
+// this thread (lane t of TPP); in the tile that holds them (SELF), each
+// particle skips its own record self[k].
 template <class T, int TPP, bool SELF>
-__device__ __forceinline__ void dyn_tile(const Dyn<T> *tile, int count, int self, int t, T rx,
-                                         T ry, T rz, T &ex, T &ey, T &ez, T &bx, T &by, T &bz)
+__device__ __forceinline__ void dyn_tile(const Dyn<T> *tile, int count, const int (&self)[kParts],
+                                         int t, const T (&rx)[kParts], const T (&ry)[kParts],
+                                         const T (&rz)[kParts], T (&ex)[kParts], T (&ey)[kParts],
+                                         T (&ez)[kParts], T (&bx)[kParts], T (&by)[kParts],
+                                         T (&bz)[kParts])
 {
-#pragma unroll 4
+#pragma unroll 2
     for (int j = t; j < count; j += TPP) {
-        if (SELF && j == self)
-            continue;
         const Dyn<T> d = tile[j];
-        const T dx = rx - d.x, dy = ry - d.y, dz = rz - d.z;
-        const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-        const T w = d.q * inv_len3<T>(r2);
-        ex = fma(w, dx, ex);
-        ey = fma(w, dy, ey);
-        ez = fma(w, dz, ez);
-        // v_j x r
-        const T cx = fma(d.vy, dz, -d.vz * dy);
-        const T cy = fma(d.vz, dx, -d.vx * dz);
-        const T cz = fma(d.vx, dy, -d.vy * dx);
-        bx = fma(w, cx, bx);
-        by = fma(w, cy, by);
-        bz = fma(w, cz, bz);
+#pragma unroll
+        for (int k = 0; k < kParts; ++k) {
+            if (SELF && j == self[k])
+                continue;
+            const T dx = rx[k] - d.x, dy = ry[k] - d.y, dz = rz[k] - d.z;
+            const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+            const T w = d.q * inv_len3<T>(r2);
+            ex[k] = fma(w, dx, ex[k]);
+            ey[k] = fma(w, dy, ey[k]);
+            ez[k] = fma(w, dz, ez[k]);
+            // v_j x r
+            const T cx = fma(d.vy, dz, -d.vz * dy);
+            const T cy = fma(d.vz, dx, -d.vx * dz);
+            const T cz = fma(d.vx, dy, -d.vy * dx);
+            bx[k] = fma(w, cx, bx[k]);
+            by[k] = fma(w, cy, by[k]);
+            bz[k] = fma(w, cz, bz[k]);
+        }
     }
 }
 
@@ -99,115 +117,142 @@ template <int TPP, class T> __device__ __forceinline__ T lanes_sum(T v)
 }
 
 // TPP lanes share a particle and split its sums (j = t, t + TPP, ...), so a
-// modest particle count still fills the SMs; a block holds kVerletBlock/TPP
-// particles, all in one 128-record particle tile.
+// modest particle count still fills the SMs; a thread holds kParts
+// particles (slot s of the block: particles s, s + S, s + 2S, ... with
+// S = kVerletBlock/TPP), a block kParts S particles, all in one
+// kTile-record tile.
 template <class T, int TPP>
 __global__ void __launch_bounds__(kVerletBlock) verlet_kernel(const VerletArgs<T> A)
 {
-    __shared__ Dyn<T> dtile[kVerletBlock];
-    __shared__ Q4<T> stile_q[kVerletBlock];
-    T *stile = &stile_q[0].x;
-    constexpr int PPB = kVerletBlock / TPP; // particles per block
+    __shared__ Dyn<T> dtile[kTile];
+    __shared__ Q4<T> stile[kTile];
+    constexpr int S = kVerletBlock / TPP; // particle slots per block
+    constexpr int PPB = kParts * S;       // particles per block
+    static_assert(kTile % PPB == 0 && kTile % TPP == 0, "tile holds whole blocks");
     const int t = threadIdx.x % TPP;
-    const int local = threadIdx.x / TPP;
-    const long long i = blockIdx.x * (long long)PPB + local;
-    const bool own = i < A.n;
-    Dyn<T> me{};
-    T ax = 0, ay = 0, az = 0;
-    if (own) {
-        me = A.in[i];
-        ax = A.accel[3 * i];
-        ay = A.accel[3 * i + 1];
-        az = A.accel[3 * i + 2];
-    }
+    const int slot = threadIdx.x / TPP;
+    const long long base = blockIdx.x * (long long)PPB;
+    long long i[kParts];
+    bool own[kParts];
+    T q[kParts], mass[kParts];
+    T rx[kParts], ry[kParts], rz[kParts], vx[kParts], vy[kParts], vz[kParts];
     const T dt2 = A.dt / T(2);
-    // v(t + dt/2) = v(t) + a(t) dt/2;  r(t + dt) = r(t) + v(t + dt/2) dt
-    T vx = me.vx + ax * dt2, vy = me.vy + ay * dt2, vz = me.vz + az * dt2;
-    T rx = me.x + vx * A.dt, ry = me.y + vy * A.dt, rz = me.z + vz * A.dt;
+#pragma unroll
+    for (int k = 0; k < kParts; ++k) {
+        i[k] = base + slot + (long long)k * S;
+        own[k] = i[k] < A.n;
+        Dyn<T> me{};
+        T ax = 0, ay = 0, az = 0;
+        if (own[k]) {
+            me = A.in[i[k]];
+            ax = A.accel[3 * i[k]];
+            ay = A.accel[3 * i[k] + 1];
+            az = A.accel[3 * i[k] + 2];
+        }
+        q[k] = me.q;
+        mass[k] = me.m;
+        // v(t + dt/2) = v(t) + a(t) dt/2;  r(t + dt) = r(t) + v(t + dt/2) dt
+        vx[k] = me.vx + ax * dt2;
+        vy[k] = me.vy + ay * dt2;
+        vz[k] = me.vz + az * dt2;
+        rx[k] = me.x + vx[k] * A.dt;
+        ry[k] = me.y + vy[k] * A.dt;
+        rz[k] = me.z + vz[k] * A.dt;
+    }
 
-    T ex = 0, ey = 0, ez = 0, bx = 0, by = 0, bz = 0;
-    for (int t0 = 0; t0 < A.p; t0 += kVerletBlock) {
-        const int cnt = min(kVerletBlock, A.p - t0);
+    T ex[kParts], ey[kParts], ez[kParts], bx[kParts], by[kParts], bz[kParts];
+#pragma unroll
+    for (int k = 0; k < kParts; ++k)
+        ex[k] = ey[k] = ez[k] = bx[k] = by[k] = bz[k] = 0;
+    for (int t0 = 0; t0 < A.p; t0 += kTile) {
+        const int cnt = min(kTile, A.p - t0);
         __syncthreads();
         for (int k = threadIdx.x; k < cnt; k += kVerletBlock)
-            reinterpret_cast<Q4<T> *>(stile)[k] = reinterpret_cast<const Q4<T> *>(A.charges)[t0 + k];
+            stile[k] = reinterpret_cast<const Q4<T> *>(A.charges)[t0 + k];
         __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
         for (int j = t; j < cnt; j += TPP) {
-            const Q4<T> c = reinterpret_cast<const Q4<T> *>(stile)[j];
-            const T dx = rx - c.x, dy = ry - c.y, dz = rz - c.z;
-            const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-            const T w = c.q * inv_len3<T>(r2);
-            ex = fma(w, dx, ex);
-            ey = fma(w, dy, ey);
-            ez = fma(w, dz, ez);
+            const Q4<T> c = stile[j];
+#pragma unroll
+            for (int k = 0; k < kParts; ++k) {
+                const T dx = rx[k] - c.x, dy = ry[k] - c.y, dz = rz[k] - c.z;
+                const T r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+                const T w = c.q * inv_len3<T>(r2);
+                ex[k] = fma(w, dx, ex[k]);
+                ey[k] = fma(w, dy, ey[k]);
+                ez[k] = fma(w, dz, ez[k]);
+            }
         }
     }
-    const long long mine = (blockIdx.x * (long long)PPB) / kVerletBlock * kVerletBlock;
-    const int self = (int)(i - mine);
-    for (long long t0 = 0; t0 < A.n; t0 += kVerletBlock) {
-        const int cnt = (int)min((long long)kVerletBlock, A.n - t0);
+    const long long mine = base / kTile * kTile; // the tile holding this block
+    int self[kParts];
+#pragma unroll
+    for (int k = 0; k < kParts; ++k)
+        self[k] = (int)(i[k] - mine);
+    for (long long t0 = 0; t0 < A.n; t0 += kTile) {
+        const int cnt = (int)min((long long)kTile, A.n - t0);
         __syncthreads();
-        if (threadIdx.x < cnt)
-            dtile[threadIdx.x] = A.in[t0 + threadIdx.x];
+        for (int k = threadIdx.x; k < cnt; k += kVerletBlock)
+            dtile[k] = A.in[t0 + k];
         __syncthreads();
         if (t0 == mine)
             dyn_tile<T, TPP, true>(dtile, cnt, self, t, rx, ry, rz, ex, ey, ez, bx, by, bz);
         else
-            dyn_tile<T, TPP, false>(dtile, cnt, -1, t, rx, ry, rz, ex, ey, ez, bx, by, bz);
+            dyn_tile<T, TPP, false>(dtile, cnt, self, t, rx, ry, rz, ex, ey, ez, bx, by, bz);
     }
-    ex = lanes_sum<TPP>(ex);
-    ey = lanes_sum<TPP>(ey);
-    ez = lanes_sum<TPP>(ez);
-    bx = lanes_sum<TPP>(bx);
-    by = lanes_sum<TPP>(by);
-    bz = lanes_sum<TPP>(bz);
-    if (!own || t != 0)
-        return;
     const T K = (T)kElectroK, MK = (T)kMagnetoK;
-    ex *= K;
-    ey *= K;
-    ez *= K;
-    bx *= MK;
-    by *= MK;
-    bz *= MK;
-    // a = (q E + q v x B) / m
-    const T fx = me.q * ex + me.q * (vy * bz - vz * by);
-    const T fy = me.q * ey + me.q * (vz * bx - vx * bz);
-    const T fz = me.q * ez + me.q * (vx * by - vy * bx);
-    ax = fx / me.m;
-    ay = fy / me.m;
-    az = fz / me.m;
-    vx += ax * dt2;
-    vy += ay * dt2;
-    vz += az * dt2;
-    // BoundToBox (Particle_System.cpp:28-66): upper walls, then lower walls
-    T *r[3] = {&rx, &ry, &rz}, *v[3] = {&vx, &vy, &vz};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        if (*r[c] > A.hi[c]) {
-            *r[c] = T(2) * A.hi[c] - *r[c];
-            *v[c] = -*v[c];
-        }
-    }
+    for (int k = 0; k < kParts; ++k) {
+        T Ex = lanes_sum<TPP>(ex[k]), Ey = lanes_sum<TPP>(ey[k]), Ez = lanes_sum<TPP>(ez[k]);
+        T Bx = lanes_sum<TPP>(bx[k]), By = lanes_sum<TPP>(by[k]), Bz = lanes_sum<TPP>(bz[k]);
+        if (!own[k] || t != 0)
+            continue;
+        Ex *= K;
+        Ey *= K;
+        Ez *= K;
+        Bx *= MK;
+        By *= MK;
+        Bz *= MK;
+        T vxk = vx[k], vyk = vy[k], vzk = vz[k];
+        T rxk = rx[k], ryk = ry[k], rzk = rz[k];
+        // a = (q E + q v x B) / m
+        const T fx = q[k] * Ex + q[k] * (vyk * Bz - vzk * By);
+        const T fy = q[k] * Ey + q[k] * (vzk * Bx - vxk * Bz);
+        const T fz = q[k] * Ez + q[k] * (vxk * By - vyk * Bx);
+        const T axk = fx / mass[k], ayk = fy / mass[k], azk = fz / mass[k];
+        vxk += axk * dt2;
+        vyk += ayk * dt2;
+        vzk += azk * dt2;
+        // BoundToBox (Particle_System.cpp:28-66): upper walls, then lower walls
+        T *r[3] = {&rxk, &ryk, &rzk}, *v[3] = {&vxk, &vyk, &vzk};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        if (*r[c] < A.lo[c]) {
-            *r[c] = T(2) * A.lo[c] - *r[c];
-            *v[c] = -*v[c];
+        for (int c = 0; c < 3; ++c) {
+            if (*r[c] > A.hi[c]) {
+                *r[c] = T(2) * A.hi[c] - *r[c];
+                *v[c] = -*v[c];
+            }
         }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (*r[c] < A.lo[c]) {
+                *r[c] = T(2) * A.lo[c] - *r[c];
+                *v[c] = -*v[c];
+            }
+        }
+        Dyn<T> o;
+        o.q = q[k];
+        o.m = mass[k];
+        o.x = rxk;
+        o.y = ryk;
+        o.z = rzk;
+        o.vx = vxk;
+        o.vy = vyk;
+        o.vz = vzk;
+        A.out[i[k]] = o;
+        A.accel[3 * i[k]] = axk;
+        A.accel[3 * i[k] + 1] = ayk;
+        A.accel[3 * i[k] + 2] = azk;
     }
-    Dyn<T> o = me;
-    o.x = rx;
-    o.y = ry;
-    o.z = rz;
-    o.vx = vx;
-    o.vy = vy;
-    o.vz = vz;
-    A.out[i] = o;
-    A.accel[3 * i] = ax;
-    A.accel[3 * i + 1] = ay;
-    A.accel[3 * i + 2] = az;
 }
 
 template <class T>
@@ -272,21 +317,29 @@ int verlet(T *dyn, T *accel, size_t n, const T *charges, size_t p, const T *box_
         A.hi[k] = box_max[k];
     }
     A.dt = dt;
-    // lanes per particle: the caller's (opt->threads_per_line), else enough
-    // threads for about 48 warps per SM
-    const size_t want = (size_t)c.nsm * 48 * 32;
-    int tpp = n * 2 <= want ? 4 : n <= want ? 2 : 1;
+    // lanes per particle: the caller's (opt->threads_per_line), else the
+    // fewest that give about 24 warps per SM (kParts particles per thread)
+    const size_t want = (size_t)c.nsm * 24 * 32;
+    int tpp = 8;
+    for (int cand = 1; cand <= 4; cand *= 2)
+        if (n * cand / kParts >= want) {
+            tpp = cand;
+            break;
+        }
     if (o.threads_per_line)
         tpp = o.threads_per_line;
-    if (tpp != 1 && tpp != 2 && tpp != 4)
+    if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8)
         return EM_ERR_ARG;
-    const unsigned grid = (unsigned)((n * tpp + kVerletBlock - 1) / kVerletBlock);
+    const size_t ppb = (size_t)kParts * kVerletBlock / tpp; // particles per block
+    const unsigned grid = (unsigned)((n + ppb - 1) / ppb);
     if (e == cudaSuccess)
         e = cudaEventRecord(c.ev0, s);
     for (size_t k = 0; k < steps && e == cudaSuccess; ++k) {
         A.in = buf[k & 1];
         A.out = buf[(k + 1) & 1];
-        if (tpp == 4)
+        if (tpp == 8)
+            verlet_kernel<T, 8><<<grid, kVerletBlock, 0, s>>>(A);
+        else if (tpp == 4)
             verlet_kernel<T, 4><<<grid, kVerletBlock, 0, s>>>(A);
         else if (tpp == 2)
             verlet_kernel<T, 2><<<grid, kVerletBlock, 0, s>>>(A);
