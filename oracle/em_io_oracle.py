@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT.
 
 Restatement, in numpy, of the reference program's inputs and outputs around
-the tracer, used as the checker of the library's versions:
+the tracer, the oracle the tests hold the library's versions to:
 
   PRESETS          SimulationParams of ElectroMag/src/ElectroMag.cpp:43-55
   init_charges     InitializePointChargeArray, "Electromag utils.h":91-111

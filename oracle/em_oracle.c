@@ -3,7 +3,7 @@
  *
  * Portable-C restatement of the ElectroMag field-line tracer (reference:
  * ElectroMag/src/CPU_Implement.cpp, include/Electrostatics.h,
- * include/Vector.h).  Used only as the checker by the tests, by the smoke
+ * include/Vector.h).  The oracle: used only by the tests, by the smoke
  * check and as bench.py's CPU baseline.  Compile with -ffp-contract=off and
  * without -ffast-math: the operation sequence below is the reference's, one
  * IEEE-754 rounding per operation, so that the results are bit-identical to
