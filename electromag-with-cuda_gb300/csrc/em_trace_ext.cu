@@ -691,6 +691,17 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
     __syncthreads(); // first lines taken
     take();
 
+    // this warp's W-th of the resident set (and of the re-evaluation's
+    // records), of a full wide tile and of the last, shorter one: fixed for
+    // the whole launch, so no division per row or tile
+    const int pb = (int)((long long)P.p_pad * wg / W);
+    const int pe = (int)((long long)P.p_pad * (wg + 1) / W);
+    const int last_recs = P.p_pad - (P.n_tiles - 1) * P.tile_recs;
+    const int tb_ = (int)((long long)P.tile_recs * wg / W);
+    const int te = (int)((long long)P.tile_recs * (wg + 1) / W);
+    const int lb = (int)((long long)last_recs * wg / W);
+    const int le = (int)((long long)last_recs * (wg + 1) / W);
+
     uint32_t it = 0;
     bool failed = false;
     bool in_ring = true; // streamed: still consuming the tile ring
@@ -722,12 +733,10 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
         float dall = 3.0e38f;
         CF hx, hy, hz;
         if (!streamed) {
-            const int b = (int)((long long)P.p_pad * wg / W);
-            const int e = (int)((long long)P.p_pad * (wg + 1) / W);
-            const int jn = min(max(jneg_all - b, 0), e - b);
+            const int jn = min(max(jneg_all - pb, 0), pe - pb);
             if (live)
-                tile_pairs<T, MODE>(32, tiles + b, jn, e - b, lane, st, ax, ay, az, dneg, dall,
-                                    hx, hy, hz);
+                tile_pairs<T, MODE>(32, tiles + pb, jn, pe - pb, lane, st, ax, ay, az, dneg,
+                                    dall, hx, hy, hz);
         } else {
             for (int tile = 0; in_ring && tile < P.n_tiles; ++tile, ++it) {
                 const uint32_t sg = it % NST, ph = (it / NST) & 1;
@@ -735,10 +744,9 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
                     failed = true;
                 if (!failed) {
                     const int base = tile * P.tile_recs;
-                    const int recs = min(P.tile_recs, P.p_pad - base);
-                    const int b = (int)((long long)recs * wg / W);
-                    const int e = (int)((long long)recs * (wg + 1) / W);
-                    const int jt = min(max(jneg_all - base, 0), recs);
+                    const bool last_tile = tile == P.n_tiles - 1;
+                    const int b = last_tile ? lb : tb_, e = last_tile ? le : te;
+                    const int jt = min(max(jneg_all - base, 0), P.tile_recs);
                     const int jn = min(max(jt - b, 0), e - b);
                     if (live)
                         tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane, st,
@@ -827,8 +835,7 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
                 const bool gredo = grp_flag[g] == 2;
                 double fx = 0, fy = 0, fz = 0;
                 if (gredo) {
-                    const int cb = (int)((long long)P.p_pad * wg / W);
-                    const int ce = (int)((long long)P.p_pad * (wg + 1) / W);
+                    const int cb = pb, ce = pe;
                     const float4 *cr = reinterpret_cast<const float4 *>(P.charges) + cb;
                     if (P.refine_df64)
                         field_df64<32>(cr, ce - cb, lane, (float)st.px, (float)st.py,
