@@ -2,8 +2,8 @@
 
 Times the batched launch on a sample of the caller's charge sets over the
 shape parameters - lanes per line, lines per work item (lines per CTA at a
-time), first-phase step budget, charge-tile size and pipeline stages of the
-sets streamed through shared memory - by coordinate descent from the
+time), charge-tile size and pipeline stages of the sets streamed through
+shared memory - by coordinate descent from the
 library's defaults, and caches the winner per GPU and workload signature in
 a JSON file (EM_AUTOTUNE_CACHE, default: autotune_cache.json beside this
 module).
@@ -20,10 +20,13 @@ CACHE = os.environ.get("EM_AUTOTUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                     "autotune_cache.json"))
 
+# The first phase's step budget is not searched (it stays the library's
+# 64): on sets cut to a sample's line counts a larger budget looked 5-10 %
+# faster, on the whole 512-set batch it was 20 % slower (its phases carry
+# far more lines than the sample's).
 SPACE = {
     "threads_per_line": [16, 8, 4],
     "lines_per_item": [512, 256, 1024],
-    "first_budget": [64, 32, 128, 256, 512],
     "tile_charges": [1024, 2048, 512],
     "stages": [4, 3, 2],
 }
@@ -63,6 +66,22 @@ def _time(sets, max_steps, lims, opts, repeats=2):
     return best
 
 
+def _sample(sets, steps_per_line, n, seed, lines_cap, cap):
+    """`n` sets drawn at random, each cut to its first `lines_cap` lines,
+    with their step limits (capped at `cap`)."""
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(len(sets), min(n, len(sets)), replace=False))
+    sub = [(sets[i][0], sets[i][1][:lines_cap]) for i in idx]
+    lims = None
+    if steps_per_line is not None:
+        offs = np.concatenate([[0], np.cumsum([len(s) for _, s in sets])])
+        lims = np.concatenate([
+            np.minimum(steps_per_line[offs[i]:offs[i] + min(lines_cap,
+                                                           offs[i + 1] - offs[i])],
+                       cap) for i in idx]).astype(np.int32)
+    return sub, lims
+
+
 def tune_batch(sets, max_steps, steps_per_line=None, sample=32, seed=0,
                rounds=2, use_cache=True, lines_cap=1024, steps_cap=None):
     """Returns the best option dict for trace_batch on these sets.
@@ -71,24 +90,19 @@ def tune_batch(sets, max_steps, steps_per_line=None, sample=32, seed=0,
     `lines_cap` lines: the same mix of set sizes and the same step limits (a
     few long lines carry most of the pairs, and the phase budgets are tuned
     for them, so steps are not capped unless `steps_cap` is given) at a
-    fraction of the cost."""
+    fraction of the cost.  A sample of cut sets is noisy and may misjudge the
+    whole batch (its phases carry fewer lines), so a step of the descent must
+    gain 3 % and the winner must beat the defaults by 5 % on a second,
+    independent sample; otherwise the defaults stand."""
     key = _device_key() + "|" + _signature(sets, max_steps)
     cache = _load() if use_cache else {}
     if key in cache:
         return dict(cache[key]["options"])
-    rng = np.random.default_rng(seed)
-    idx = np.sort(rng.choice(len(sets), min(sample, len(sets)), replace=False))
-    sub = [(sets[i][0], sets[i][1][:lines_cap]) for i in idx]
     cap = max_steps if steps_cap is None else steps_cap
-    lims = None
-    if steps_per_line is not None:
-        offs = np.concatenate([[0], np.cumsum([len(s) for _, s in sets])])
-        lims = np.concatenate([
-            np.minimum(steps_per_line[offs[i]:offs[i] + min(lines_cap,
-                                                           offs[i + 1] - offs[i])],
-                       cap) for i in idx]).astype(np.int32)
+    sub, lims = _sample(sets, steps_per_line, sample, seed, lines_cap, cap)
     max_steps = min(max_steps, cap)
-    best = {k: v[0] for k, v in SPACE.items()}
+    default = {k: v[0] for k, v in SPACE.items()}
+    best = dict(default)
     best_t = _time(sub, max_steps, lims, best)
     trials = [(dict(best), best_t)]
     for _ in range(rounds):
@@ -100,10 +114,15 @@ def tune_batch(sets, max_steps, steps_per_line=None, sample=32, seed=0,
                 cand = dict(best, **{k: v})
                 t = _time(sub, max_steps, lims, cand)
                 trials.append((cand, t))
-                if t < best_t * 0.98:
+                if t < best_t * 0.97:
                     best, best_t, changed = cand, t, True
         if not changed:
             break
+    if best != default:
+        vsub, vlims = _sample(sets, steps_per_line, sample, seed + 1, lines_cap, cap)
+        if not (_time(vsub, max_steps, vlims, best)
+                < 0.95 * _time(vsub, max_steps, vlims, default)):
+            best = dict(default)
     if use_cache:
         cache[key] = {"options": best, "seconds": best_t,
                       "trials": len(trials)}

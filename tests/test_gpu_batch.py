@@ -98,3 +98,23 @@ def test_batch_widening_agrees(em, gpu, batch_case, orc):
     b = em.trace_batch(sets, 300, 1.0, 0.5, steps_per_line=lims)
     agree = (a["cls"] == b["cls"]).mean()
     assert agree >= 0.999, agree
+
+
+def test_autotuner_returns_a_working_shape(em, gpu, batch_case):
+    """The tuner's answer is a complete option dict from its search space
+    (the defaults unless a candidate also wins on a second sample), and a
+    batch run with it equals the per-set calls."""
+    sets, lims = batch_case
+    opts = em.autotune.tune_batch(sets, 300, lims, sample=6, use_cache=False,
+                                  rounds=1)
+    assert set(opts) == set(em.autotune.SPACE)
+    for k, v in opts.items():
+        assert v in em.autotune.SPACE[k]
+    b = em.trace_batch(sets, 300, 1.0, 0.5, steps_per_line=lims,
+                       deterministic=True, **opts)
+    ref = per_set(em, sets, 300, lims, 0, tpl=opts["threads_per_line"])
+    k = 0
+    for (ch, seeds), r in zip(sets, ref):
+        m = len(seeds)
+        assert np.array_equal(b["len"][k:k + m], r["len"])
+        k += m
