@@ -170,18 +170,20 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
         }
     }
     // with resident charges a warp's share of a row must outweigh the two
-    // warp reductions and the barriers per row: at least 32 FP32 pairs per
-    // lane (about 14 instructions each), 24 mixed, 12 double-float (about
-    // 150), 2 FP64 (1/64 rate); below two warps per line the lane-group
-    // kernel's regrouping (a warp per line) serves the tail better.
-    // Streamed rows also wait on the tile ring, so there the count alone
-    // sets W.
+    // warp reductions and the barriers per row: at least 8 FP32 pairs per
+    // lane (about 14 instructions each), 6 mixed or double-float, 1 FP64
+    // (measured on the GPU-scale set with termination: 32 / 24 / 12 pairs
+    // gave 14.4 / 31.5 / 57 ms for FP32 / mixed / double-float, 16 / 12 / 6
+    // gave 12.8 / 25.7 / 54, 8 / 6 / 3 gave 12.0 / 23.0 / 55); below two
+    // warps per line the lane-group kernel's regrouping (a warp per line)
+    // serves the tail better.  Streamed rows also wait on the tile ring, so
+    // there the count alone sets W.
     int w_cap = wcfg.warps;
     if (cfg.resident) {
-        const long long per_lane = sizeof(T) == 8       ? 2
-                                   : mode == EXT_DF64  ? 12
-                                   : mode == EXT_MIXED ? 24
-                                                       : 32;
+        const long long per_lane = sizeof(T) == 8       ? 1
+                                   : mode == EXT_DF64  ? 6
+                                   : mode == EXT_MIXED ? 6
+                                                       : 8;
         w_cap = (int)std::min<long long>(wcfg.warps, p_pad / (32LL * per_lane));
     }
     const bool tail = !o.deterministic && !o.warps_per_cta && w_cap >= 2 &&
