@@ -49,6 +49,21 @@ def test_reference_codes_before_any_device_work(em, n, steps, res, curv, want):
     assert rc == want
 
 
+@pytest.mark.parametrize("dtype,kw", [
+    (np.float64, dict(arith="mixed")),          # mixed arithmetic is FP32-only
+    (np.float32, dict(arith="mixed", null_frac=-1.0)),
+])
+def test_option_errors_before_any_device_work(em, dtype, kw):
+    """Option errors are argument errors (code 4), answered before the
+    device is touched."""
+    n, steps = 64, 4
+    x = np.zeros(n * steps, dtype)
+    y, z = x.copy(), x.copy()
+    ch = np.zeros((4, 4), dtype)
+    rc, _ = em.calc_field(x, y, z, ch, n, 1.0, True, **kw)
+    assert rc == 4
+
+
 def test_dropin_header_compiles_against_stand_in_types(tmp_path):
     """include/emgb300_dropin.hpp (the CalcField_CPU / CalcField overloads)
     compiles and links against libemgb300.so with containers shaped like
