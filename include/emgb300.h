@@ -108,7 +108,8 @@ typedef struct em_options {
                              initial lane group, so results repeat bit for
                              bit; 0 (default) lets warps widen the groups of
                              their last lines once no lines are left to hand
-                             out (faster tails, last-bit differences)        */
+                             out, and hands the last lines to several warps
+                             each (faster tails, last-bit differences)       */
     int adjoint_checkpoint; /* em_adjoint_f32: 0 (default) keeps the forward's
                              field at every vertex (12 more bytes per vertex);
                              1 keeps only the vertices and recomputes the
