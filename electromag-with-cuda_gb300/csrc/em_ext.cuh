@@ -162,7 +162,7 @@ __device__ __forceinline__ void field_fp64(const float4 *charges, int count, int
 // two-sum, Dekker's fast two-sum, the FMA two-product), every operation an
 // explicitly rounded intrinsic so nothing is contracted.  The evaluation
 // point is an FP32 vertex, so r = p - c is exact as a pair; the pair term
-// q r / |r|^3 is formed to about 2^-42 relative, on the FP32 pipes only
+// q r / |r|^3 is formed to about 2^-41 relative, on the FP32 pipes only
 // (GB300 runs FP64 at 1/64 of the FP32 rate).
 struct DF {
     float h, l;
@@ -227,7 +227,7 @@ __device__ __forceinline__ DF df_mul_raw(DF a, DF b)
 //   high words summed by two-sums and the low words added plainly (about
 //   2^-46 relative); y0 = rsqrt(|r|^2) in FP32 and eps = 1 - |r|^2 y0^2 in
 //   double-float, so |r|^-3 = y0^3 (1 - eps)^(-3/2) = y0^3 (1 + 1.5 eps)
-//   to within 15/8 eps^2 (|eps| < 2^-21: about 2^-42 relative).
+//   to within 15/8 eps^2 (|eps| below about 2^-21.9: about 2^-41 relative).
 __device__ __forceinline__ void df_pair(float px, float py, float pz, const float4 &c, DF &tx,
                                         DF &ty, DF &tz, float &r2h)
 {
