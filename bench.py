@@ -394,6 +394,10 @@ def main():
                      "algorithmic_bytes": 12.0 * n * (rows - 1),
                      "peak_source": "measured FFMA peak (em_fp32_peak_tflops)",
                      "flop_per_pair": FLOP_PER_PAIR,
+                     # the reference's own count (perfPacket): 18 FLOP per
+                     # pair and 13 per vertex step
+                     "achieved_reference_convention":
+                         (18.0 * pairs + 13.0 * n * (rows - 1)) / kernel_s / 1e12,
                      "kernel_ms": kernel_s * 1e3},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
