@@ -233,10 +233,12 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     const bool chunked = !o.device_ptrs && nl == n && elems * sizeof(T) * 3 >= (64u << 20) &&
                          total_steps >= 64 && pl.arith != ARITH_MIXED;
     const int nchunks = chunked ? 8 : 1;
-    e = cudaEventRecord(c.ev0, s);
-    for (int k = 0; k < nchunks && e == cudaSuccess; ++k) {
-        const int r0 = 1 + (int)(((long long)(total_steps - 1) * k) / nchunks);
-        const int r1 = 1 + (int)(((long long)(total_steps - 1) * (k + 1)) / nchunks);
+    // first row of chunk k (chunk k holds rows [row_of(k), row_of(k + 1)))
+    auto row_of = [&](int k) {
+        return 1 + (int)(((long long)(total_steps - 1) * k) / nchunks);
+    };
+    auto launch_chunk = [&](int k) {
+        const int r0 = row_of(k), r1 = row_of(k + 1);
         // rows [r0, r1) from row r0 - 1: the arrays seen from row r0 - 1
         RefTraceParams<T> q = prm;
         const size_t base = (size_t)(r0 - 1) * n;
@@ -247,12 +249,29 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         q.seed_y = dy;
         q.seed_z = dz;
         q.total_steps = r1 - r0 + 1;
-        e = launch_ref_trace<T>(q, pl.cfg, pl.arith, s);
-        if (e == cudaSuccess && chunked) {
+        cudaError_t le = launch_ref_trace<T>(q, pl.cfg, pl.arith, s);
+        // the kernel time ends with the last chunk, before any copy waits
+        if (le == cudaSuccess && k == nchunks - 1)
+            le = cudaEventRecord(c.ev1, s);
+        return le;
+    };
+    e = cudaEventRecord(c.ev0, s);
+    if (e == cudaSuccess)
+        e = launch_chunk(0);
+    for (int k = 0; k < nchunks && e == cudaSuccess; ++k) {
+        // The copies of chunk k wait for chunk k alone, and chunk k + 1 is
+        // queued before them: a copy into pageable host memory returns only
+        // once it is done, and the next chunk then already runs beside it.
+        if (chunked) {
             e = cudaEventRecord(c.ev_chunk, s);
             if (e == cudaSuccess)
                 e = cudaStreamWaitEvent(c.copy_stream, c.ev_chunk, 0);
-            const size_t off = (size_t)r0 * n, cnt = (size_t)(r1 - r0) * n;
+        }
+        if (e == cudaSuccess && k + 1 < nchunks)
+            e = launch_chunk(k + 1);
+        if (e == cudaSuccess && chunked) {
+            const size_t off = (size_t)row_of(k) * n;
+            const size_t cnt = (size_t)(row_of(k + 1) - row_of(k)) * n;
             T *dst[3] = {x, y, z};
             const T *src[3] = {dx, dy, dz};
             for (int d = 0; d < 3 && e == cudaSuccess; ++d)
@@ -260,8 +279,6 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
                                     cudaMemcpyDeviceToHost, c.copy_stream);
         }
     }
-    if (e == cudaSuccess)
-        e = cudaEventRecord(c.ev1, s);
     if (e == cudaSuccess && chunked) {
         // the call's stream waits for the last copies, so it completes as one
         e = cudaEventRecord(c.ev_chunk, c.copy_stream);
