@@ -336,7 +336,8 @@ int field_at(const T *px, const T *py, const T *pz, size_t m, const T *charges, 
         return EM_OK;
     if (!px || !py || !pz || !ex || !ey || !ez || (p && !charges))
         return EM_ERR_ARG;
-    if (p > (size_t)INT_MAX / 4 || m > (size_t)LLONG_MAX / 64)
+    // one 256-thread block per 256 points: at most 2^31 - 1 blocks
+    if (p > (size_t)INT_MAX / 4 || m > (size_t)INT_MAX * 256)
         return EM_ERR_TOO_LARGE;
     em_options o{};
     if (opt)

@@ -294,7 +294,8 @@ EM_API int em_seed_fibonacci_f32(const float *charges, size_t p,
  * goes to ex/ey/ez.  Host pointers unless opt->device_ptrs.  With
  * EM_ARITH_EXACT, opt->rule picks the PartField form: EM_RULE_SSE the
  * three-argument one (:38-51), EM_RULE_GENERIC the two-argument one (:53-60).
- * opt may be NULL (fast arithmetic, host pointers). */
+ * opt may be NULL (fast arithmetic, host pointers).  m above 2^31 * 256 - 256
+ * points or p above 2^29 charges: EM_ERR_TOO_LARGE. */
 EM_API int em_field_f32(const float *px, const float *py, const float *pz,
                         size_t m, const float *charges, size_t p, float *ex,
                         float *ey, float *ez, const em_options *opt);

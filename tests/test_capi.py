@@ -64,6 +64,27 @@ def test_option_errors_before_any_device_work(em, dtype, kw):
     assert rc == 4
 
 
+def test_size_limits_before_any_device_work(em):
+    """Sizes beyond what an entry point takes return EM_ERR_TOO_LARGE (14)
+    from the argument checks, before any buffer is read or the device is
+    touched: rows beyond 2^31 - 1 or more than 2^25 - 1 charges for a
+    trace; more than 2^29 - 1 charges or points beyond 2^31 - 1 blocks of
+    256 for the field at points."""
+    lib = em._capi.load()
+    a = np.zeros(64, np.float32)
+    P = a.ctypes.data
+    # rows beyond INT_MAX (n = 64)
+    assert lib.em_calc_field_ex_f32(P, P, P, 64, 2 ** 31, P, 1, 1.0, 1,
+                                    None, None) == 14
+    # charges beyond INT_MAX / 64 (2^25 - 1)
+    assert lib.em_calc_field_ex_f32(P, P, P, 64, 4, P, 2 ** 25, 1.0, 1,
+                                    None, None) == 14
+    # field points beyond the grid limit, charges beyond INT_MAX / 4
+    assert lib.em_field_f32(P, P, P, (2 ** 31 - 1) * 256 + 1, P, 1,
+                            P, P, P, None) == 14
+    assert lib.em_field_f32(P, P, P, 64, P, 2 ** 29, P, P, P, None) == 14
+
+
 def test_dropin_header_compiles_against_stand_in_types(tmp_path):
     """include/emgb300_dropin.hpp (the CalcField_CPU / CalcField overloads)
     compiles and links against libemgb300.so with containers shaped like
