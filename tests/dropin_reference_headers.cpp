@@ -1,4 +1,4 @@
-// The drop-in of INTEGRATION.md against the reference's own headers:
+// The reference-side drop-in built against the reference's own headers:
 // CalcField_CPU<float/double> (ElectroMag/src/"CPU Implement.h":25-30)
 // specialised as one-line forwards to emgb300::calc_field, called on the
 // reference's containers (Vector3<Array<T>>, Array<pointCharge<T>>,

@@ -110,7 +110,7 @@ REFERENCE = os.environ.get("EM_REFERENCE_DIR", "/root/reference")
     REFERENCE, "ElectroMag", "src", "CPU Implement.h")),
     reason="reference tree not present")
 def test_dropin_against_reference_headers(tmp_path):
-    """The INTEGRATION.md forwards compile against the reference's own
+    """The reference-side CalcField_CPU forwards compile against its own
     headers, link against libemgb300.so and return its argument codes."""
     src = os.path.join(ROOT, "tests", "dropin_reference_headers.cpp")
     exe = tmp_path / "dropin_ref"
