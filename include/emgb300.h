@@ -145,7 +145,10 @@ typedef struct em_options {
  * Replace CalcField_CPU<float>/<double> (CPU_Implement.cpp:501-527): same
  * layout, same codes in the same order (n == 0 -> 1, resolution == 0 -> 2,
  * curvature with n % 64 -> 5, total_steps < 2 -> 3).  total_steps is the
- * reference's fieldLines.GetSize()/n (CPU_Implement.cpp:219). */
+ * reference's fieldLines.GetSize()/n (CPU_Implement.cpp:219).  The arrays
+ * may be ordinary (pageable) memory: above 64 MB of vertices the trace runs
+ * in 8 row chunks and each chunk's copy back overlaps the next chunk, with
+ * pageable and page-locked buffers alike. */
 EM_API int em_calc_field_f32(float *x, float *y, float *z, size_t n, size_t total_steps,
                       const float *charges, size_t p, float resolution,
                       int use_curvature, em_perf *perf);
