@@ -79,12 +79,26 @@ inline double smsp_efficiency(long long w)
     return w >= 4 ? 1.0 : w == 3 ? 0.95 : w == 2 ? 0.87 : 0.68;
 }
 
+// Group-steps on the busiest SM sub-partition (4 per SM) when w warps of
+// one CTA run gpc line groups: full rounds of w warps, then a last round
+// of the groups left over, each round at the issue efficiency of the warps
+// it keeps busy (a short last round runs latency-bound).
+inline double sm_rounds_cost(long long gpc, long long w)
+{
+    const long long rounds = ceil_div(gpc, w);
+    const long long last = gpc - (rounds - 1) * w;
+    const long long full = ceil_div(w, 4), tail = ceil_div(last, 4);
+    return (double)(rounds - 1) * (double)full / smsp_efficiency(full) +
+           (double)tail / smsp_efficiency(tail);
+}
+
 // Picks threads per line, lines per lane, compute warps per CTA and the
 // grid for n lines and p charges on a device with nsm SMs (one persistent
-// CTA per SM).  The model charges each SM sub-partition (4 per SM) for the
-// warps it runs.  fixed_tpl / fixed_kl of 0 are searched; shapes are tried
-// from (8, 2) down and a later one must be 2 % cheaper to replace an
-// earlier one.
+// CTA per SM).  fixed_tpl / fixed_kl of 0 are searched, and so is the warp
+// count up to max_warps (fewer warps can balance the rounds better: 54
+// groups per SM at 24 warps leave a last round of 6).  Shapes are tried
+// from (8, 2) down, most warps first, and a later one must be 2 % cheaper
+// to replace an earlier one.
 inline void choose_shape(long long n, long long p, int nsm, int max_warps, int fixed_tpl,
                          int fixed_kl, int *tpl_out, int *kl_out, int *warps_out)
 {
@@ -100,18 +114,16 @@ inline void choose_shape(long long n, long long p, int nsm, int max_warps, int f
             const long long groups = ceil_div(n, lpw);
             const long long grid = std::min<long long>(nsm, groups);
             const long long gpc = ceil_div(groups, grid);
-            const int warps = (int)std::min<long long>(max_warps, gpc);
-            const long long rounds = ceil_div(gpc, warps);
-            const long long last = gpc - (rounds - 1) * warps;
-            const double per_smsp = (double)(rounds - 1) * (double)ceil_div(warps, 4) +
-                                    (double)ceil_div(last, 4);
-            const double t = per_smsp * group_step_cost(p, tpl, kl) /
-                             smsp_efficiency(ceil_div(warps, 4));
-            if (best == 0 || t < best * 0.98) {
-                best = t;
-                bt = tpl;
-                bk = kl;
-                bw = warps;
+            const int wmax = (int)std::min<long long>(max_warps, gpc);
+            const double step = group_step_cost(p, tpl, kl);
+            for (int warps = wmax; warps >= 1; --warps) {
+                const double t = sm_rounds_cost(gpc, warps) * step;
+                if (best == 0 || t < best * 0.98) {
+                    best = t;
+                    bt = tpl;
+                    bk = kl;
+                    bw = warps;
+                }
             }
         }
     }
@@ -146,8 +158,8 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     // not say (two lines share each charge load, one line doubles the warps
     // for small line counts); 2 for packed pairs, 1 for exact arithmetic
     // (mixed: 1 unless asked; two lines' compensated sums and FP64
-    // positions do not fit the 80 registers of a 768-thread CTA: 1536
-    // against 1732 Gpair/s on 32 736 lines x 4096 charges)
+    // positions do not fit the 80 registers of a 768-thread CTA: 1534
+    // against 1731 Gpair/s at 24 warps on 32 736 lines x 4096 charges)
     int fixed_kl = 1;
     if (arith == ARITH_FAST)
         fixed_kl = o.lines_per_thread;
