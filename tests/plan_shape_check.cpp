@@ -49,6 +49,10 @@ int main()
     o.arith = EM_ARITH_MIXED;
     expect("mixed", make_plan<float>(c, 32736, 4096, o, &p) == EM_OK && p.cfg.tpl == 8 &&
                         p.cfg.kl == 1 && p.cfg.warps == 20 && p.arith == ARITH_MIXED);
+    // 16 384 lines x 1024 charges: the same 20 warps (1415 Gpair/s against
+    // 1345 at 24)
+    expect("mixed 16384x1024", make_plan<float>(c, 16384, 1024, o, &p) == EM_OK &&
+                                   p.cfg.tpl == 8 && p.cfg.kl == 1 && p.cfg.warps == 20);
     expect("mixed fp64 rejected", make_plan<double>(c, 32736, 4096, o, &p) == EM_ERR_ARG);
     o.arith = EM_ARITH_FAST;
     // 20 000 charges do not fit: streamed tiles, a producer warp's room left
