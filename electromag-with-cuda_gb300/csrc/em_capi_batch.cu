@@ -58,6 +58,9 @@ int trace_batch(size_t nsets, const float *charges, const int64_t *charge_off, c
     const int tpl = o.threads_per_line ? o.threads_per_line : 16;
     if (tpl != 4 && tpl != 8 && tpl != 16)
         return EM_ERR_ARG;
+    // a tile beyond 65 536 records could never fit shared memory
+    if (o.tile_charges < 0 || o.tile_charges > 65536)
+        return EM_ERR_ARG;
     const int item_lines = o.lines_per_item > 0 ? o.lines_per_item : 512;
     // most lines of a set end within a few dozen steps while the few that
     // run to their limit carry most of the pairs: a short first phase hands

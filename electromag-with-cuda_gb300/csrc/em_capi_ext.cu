@@ -59,6 +59,11 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     const int tpl = o.threads_per_line ? o.threads_per_line : 8;
     if (tpl != 4 && tpl != 8 && tpl != 16 && tpl != 32)
         return EM_ERR_ARG;
+    // launch-shape overrides (0: the library's choice); a tile beyond 65 536
+    // records could never fit shared memory
+    if (o.warps_per_cta < 0 || o.warps_per_cta > 32 || o.tile_charges < 0 ||
+        o.tile_charges > 65536)
+        return EM_ERR_ARG;
     if (perf)
         perf->progress = 0;
 

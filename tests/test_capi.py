@@ -64,6 +64,28 @@ def test_option_errors_before_any_device_work(em, dtype, kw):
     assert rc == 4
 
 
+@pytest.mark.parametrize("kw", [
+    dict(warps_per_cta=-1), dict(warps_per_cta=33), dict(tile_charges=-1),
+    dict(tile_charges=1 << 20), dict(threads_per_line=2)])
+def test_extended_shape_overrides_checked_before_any_device_work(em, kw):
+    """The extended tracer refuses launch-shape overrides it cannot run
+    (code 4) before the device is touched; a tile of -1 records used to
+    round to a zero tile."""
+    seeds = np.zeros((8, 3), np.float32)
+    ch = np.array([[0, 0, 0, 1]], np.float32)
+    with pytest.raises(em.EmError) as e:
+        em.trace_lines(seeds, ch, 4, 1.0, 0.5, **kw)
+    assert e.value.code == 4
+
+
+@pytest.mark.parametrize("tile", [-1, 1 << 20])
+def test_batch_tile_override_checked_before_any_device_work(em, tile):
+    sets = [(np.array([[0, 0, 0, 1]], np.float32), np.ones((4, 3), np.float32))]
+    with pytest.raises(em.EmError) as e:
+        em.trace_batch(sets, 4, 1.0, 0.5, tile_charges=tile)
+    assert e.value.code == 4
+
+
 def test_size_limits_before_any_device_work(em):
     """Sizes beyond what an entry point takes return EM_ERR_TOO_LARGE (14)
     from the argument checks, before any buffer is read or the device is
