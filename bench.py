@@ -132,6 +132,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+DATA = "synthetic (seeded PCG64)"
+
+
+def workload_config(args, n, p, rows, world, arith):
+    """The workload both arms report: the same keys and values, with the
+    arithmetic each arm computes in."""
+    return {"workload": args.workload, "lines": int(n), "charges": int(p),
+            "rows": int(rows), "seed": args.seed,
+            "rule": "curvature, seed vector (CPU_Implement.cpp:207-351)",
+            "arith": arith,
+            "parallelism": f"replicas x{world}",
+            "l2": "vertex output %.2f GB per step exceeds the 129 MB L2"
+                  % (3 * 4 * n * rows / 1e9)}
+
+
 def cpu_rate(orc, ch, seeds, rows, seconds, nthreads):
     """Oracle port on host cores over a bounded sample: all charges, a
     line subset and a row count sized to take about `seconds`."""
@@ -190,10 +205,11 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sample["seconds"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "lines": int(len(seeds)),
-                   "charges": int(len(ch)), "rows": int(rows),
-                   "rule": "curvature, seed vector (CPU_Implement.cpp:207-351)"},
+        "data": DATA,
+        "config": workload_config(
+            args, len(seeds), len(ch), rows, args.gpus,
+            "the reference's FP32 SSE sequence (sqrt + divide), oracle port "
+            "on the host cores"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
                          "kind": "port",
                          "sample": f"{sample['lines']} lines x {len(ch)} charges"
@@ -379,14 +395,9 @@ def main():
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded PCG64)",
-        "config": {"workload": args.workload, "lines": n, "charges": p,
-                   "rows": rows, "seed": args.seed,
-                   "rule": "curvature, seed vector (CPU_Implement.cpp:207-351)",
-                   "arith": "fast FP32 (rsqrt + FMA)",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "vertex output %.2f GB per step exceeds the 129 MB L2"
-                         % (3 * 4 * n * rows / 1e9)},
+        "data": DATA,
+        "config": workload_config(args, n, p, rows, world,
+                                  "fast FP32 (rsqrt + FMA)"),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops,
                      "unit": "TFLOP/s", "frac": achieved / peak_tflops,
                      "traffic": (TRAFFIC_GPU4096 if args.workload == "gpu_4096"
