@@ -68,7 +68,8 @@ class EmOptions(ctypes.Structure):
                 ("force_streamed", I), ("pack", I),
                 ("lines_per_thread", I), ("precision", I),
                 ("null_frac", D), ("deterministic", I),
-                ("adjoint_checkpoint", I), ("refine", I)]
+                ("adjoint_checkpoint", I), ("refine", I),
+                ("field_out", P)]
 
 
 _SIGNATURES = {

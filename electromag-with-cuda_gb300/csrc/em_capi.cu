@@ -47,6 +47,12 @@ DevCtx *get_ctx(int *code)
             *code = EM_ERR_CUDA;
             return nullptr;
         }
+        for (cudaEvent_t &ev : c.ev_rows)
+            if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                *code = EM_ERR_CUDA;
+                return nullptr;
+            }
         c.ready = true;
     }
     *code = EM_OK;
@@ -145,6 +151,8 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         return EM_ERR_TOO_LARGE;
     if (o.device_ptrs && ((uintptr_t)charges & 15))
         return EM_ERR_ARG;
+    if (o.field_out && !o.device_ptrs)
+        return EM_ERR_ARG;
     if (!nl)
         nl = n;
     if (line0 > n || nl > n - line0 || (nl != n && o.device_ptrs))
@@ -224,6 +232,11 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     prm.err = c.err;
     prm.qabs = qabs;
     prm.null_frac = o.null_frac > 0 ? o.null_frac : 1e-4;
+    if (o.field_out) {
+        prm.ox = static_cast<T *>(o.field_out);
+        prm.oy = prm.ox + n * (total_steps - 1);
+        prm.oz = prm.oy + n * (total_steps - 1);
+    }
 
     // Host arrays, all lines: trace in row chunks and copy each finished
     // chunk to the host on the copy stream while the next one is traced
@@ -253,6 +266,8 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         // the kernel time ends with the last chunk, before any copy waits
         if (le == cudaSuccess && k == nchunks - 1)
             le = cudaEventRecord(c.ev1, s);
+        if (le == cudaSuccess && chunked)
+            le = cudaEventRecord(c.ev_rows[k], s);
         return le;
     };
     e = cudaEventRecord(c.ev0, s);
@@ -308,6 +323,17 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
                                   cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess)
             return map_cuda(e);
+    }
+    // Progress while the chunks run, for a thread that polls perf->progress
+    // as the reference's monitor does ("Electromag utils.h":133-156; the
+    // reference adds each finished block's share, CPU_Implement.cpp:340-342):
+    // the share of rows traced, raised as each chunk's trace completes.
+    if (chunked && perf) {
+        for (int k = 0; k + 1 < nchunks; ++k) {
+            if (cudaEventSynchronize(c.ev_rows[k]) != cudaSuccess)
+                break; // the stream's error is reported below
+            perf->progress = (double)(row_of(k + 1) - 1) / (double)(total_steps - 1);
+        }
     }
     int dev_err = 0;
     code = read_dev_err(c, s, &dev_err);

@@ -65,6 +65,9 @@ template <class T> struct RefTraceParams {
     // mixed arithmetic: largest |q| and the re-evaluation threshold
     const float *qabs;
     double null_frac;
+    // optional: the field each step uses (Coulomb constant applied, after
+    // any re-evaluation), stored like fx (null: none)
+    T *ox, *oy, *oz;
 };
 
 // Extended tracer (em_trace_ext.cu).

@@ -16,6 +16,8 @@
 // - The first call on a device does a one-time set-up (it looks up the
 //   array's device address with cudaGetSymbolAddress, which may load this
 //   module onto the device); make that first call before any stream capture.
+// - Every call waits for its own work: it reads the kernel's error word back
+//   and synchronises `stream` before it returns.
 // - Every call on a device shares the one array and leaves its contents
 //   behind.  The error word is cleared at the start of each call; the staged
 //   charges are rewritten.  Calls whose work overlaps on the GPU (different

@@ -23,6 +23,7 @@ struct DevCtx {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr; // device-to-host copies overlapped with tracing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_chunk = nullptr;
+    cudaEvent_t ev_rows[8] = {}; // end of each row chunk's trace (progress)
     void *charges = nullptr; // staged (padded, possibly paired) charges
     size_t charges_cap = 0;
     void *charges_raw = nullptr; // the caller's records, copied as given
@@ -139,7 +140,10 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     const int fixed_tpl = o.arith == EM_ARITH_EXACT ? 1 : o.threads_per_line;
     if (fixed_tpl != 0 && fixed_tpl != 1 && fixed_tpl != 2 && fixed_tpl != 4 && fixed_tpl != 8)
         return EM_ERR_ARG;
-    if (o.warps_per_cta < 0 || o.warps_per_cta > 32 || o.tile_charges < 0)
+    // tile overrides beyond 65 536 records could never fit shared memory and
+    // would overflow the granule rounding below
+    if (o.warps_per_cta < 0 || o.warps_per_cta > 32 || o.tile_charges < 0 ||
+        o.tile_charges > 65536)
         return EM_ERR_ARG;
     if (o.pack < EM_PACK_AUTO || o.pack > EM_PACK_PAIRS)
         return EM_ERR_ARG;

@@ -398,6 +398,14 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                             az = (T)(fz * kElectroK);
                         }
                     }
+                }
+                if (P.ox && own[k] && t == 0) {
+                    const size_t fi = (size_t)(step - 1) * n + (size_t)line[k];
+                    store_stream(P.ox + fi, ax);
+                    store_stream(P.oy + fi, ay);
+                    store_stream(P.oz + fi, az);
+                }
+                if constexpr (ARITH == ARITH_MIXED) {
                     // the reference's step in FP32, the position in FP64
                     T sx, sy, sz;
                     step_of<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, sx, sy, sz);

@@ -49,7 +49,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                arith="fast", rule="sse", require_n64=None, stream=None,
                threads_per_line=0, warps_per_cta=0, tile_charges=0,
                force_streamed=False, pack="auto", lines_per_thread=0,
-               plain=None, null_frac=0.0):
+               plain=None, null_frac=0.0, field_out=None):
     """Traces n field lines in place; returns (rc, perf).
 
     arith: "fast" (FP32/FP64 rsqrt + FMA), "exact" (the reference's IEEE
@@ -61,6 +61,9 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     3 total_steps < 2, 5 n % 64 with require_n64) or a library code >= 4.
     `plain=True` calls em_calc_field_f32/_f64, the exact reference
     signature (host arrays only; the n % 64 restriction applies).
+    `field_out` (CUDA tensors only): a tensor of 3 * n * (total_steps - 1)
+    values of the arrays' type that receives the field each step used,
+    x block, y block, z block, vertex s of line l at s * n + l.
     """
     lib = _capi.load()
     dtype_name = "float32" if str(x.dtype).endswith("float32") else "float64"
@@ -77,7 +80,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                  and require_n64 in (None, True) and not threads_per_line
                  and not warps_per_cta and not tile_charges
                  and not force_streamed and pack == "auto"
-                 and not lines_per_thread)
+                 and not lines_per_thread and field_out is None)
     if plain:
         if device:
             raise ValueError("the plain entry point takes host arrays")
@@ -102,6 +105,13 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     o.pack = _PACK[pack]
     o.lines_per_thread = lines_per_thread
     o.null_frac = null_frac
+    if field_out is not None:
+        if not (_is_torch(field_out) and field_out.is_cuda and device):
+            raise ValueError("field_out needs CUDA tensors throughout")
+        _check(field_out, dtype_name)
+        if field_out.numel() < 3 * n * (total_steps - 1):
+            raise ValueError("field_out holds fewer than 3*n*(total_steps-1) values")
+        o.field_out = field_out.data_ptr()
     fn = lib.em_calc_field_ex_f32 if f32 else lib.em_calc_field_ex_f64
     rc = fn(_ptr(x), _ptr(y), _ptr(z), n, total_steps, _ptr(charges), p,
             resolution, int(bool(use_curvature)), ctypes_byref(o),

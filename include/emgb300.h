@@ -117,6 +117,12 @@ typedef struct em_options {
     int refine;           /* mixed precision: EM_REFINE_FP64 (default) or
                              EM_REFINE_DF64, the arithmetic of the field
                              re-evaluated near nulls                         */
+    void *field_out;      /* em_calc_field_ex_* with device_ptrs only
+                             (NULL: none): the field each step uses, as the
+                             arrays' type, Coulomb constant applied; three
+                             arrays of n*(total_steps-1) values back to back
+                             (x, then y, then z), the field at vertex s of
+                             line l at s*n + l                               */
 } em_options;
 
 /* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
@@ -179,8 +185,9 @@ EM_API int em_calc_field_ex_f64(double *x, double *y, double *z, size_t n,
  * Its scratch is one static device array per GPU, held until exit, sized
  * for at most EM_NOALLOC_MAX_CHARGES charges; larger sets return
  * EM_ERR_TOO_LARGE.  The first call on a device performs a one-time set-up
- * (make it before any stream capture).  All calls on a device share the
- * array: calls that overlap on the GPU race, so order them. */
+ * (make it before any stream capture).  Every call synchronises `stream`
+ * before it returns (it reads the kernel's error word back).  All calls on a
+ * device share the array: calls that overlap on the GPU race, so order them. */
 #define EM_NOALLOC_MAX_CHARGES 16384
 EM_API int em_calc_field_noalloc_f32(float *x, float *y, float *z, size_t n,
                                      size_t total_steps, const float *charges,

@@ -185,7 +185,8 @@ void orc_field_f32(const float *px, const float *py, const float *pz, size_t m,
                    float *ey, float *ez)
 {
     const float K = (float)ORC_ELECTRO_K;
-    for (size_t i = 0; i < m; ++i) {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)m; ++i) {
         float ax = 0, ay = 0, az = 0;
         for (size_t j = 0; j < p; ++j) {
             const float rx = px[i] - charges[4 * j + 0];
