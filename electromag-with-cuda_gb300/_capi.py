@@ -69,7 +69,7 @@ class EmOptions(ctypes.Structure):
                 ("lines_per_thread", I), ("precision", I),
                 ("null_frac", D), ("deterministic", I),
                 ("adjoint_checkpoint", I), ("refine", I),
-                ("field_out", P)]
+                ("field_out", P), ("refine_kappa", D)]
 
 
 _SIGNATURES = {

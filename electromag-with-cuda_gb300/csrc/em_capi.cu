@@ -144,7 +144,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         return EM_ERR_ARG;
     if (o.rule != EM_RULE_SSE && o.rule != EM_RULE_GENERIC)
         return EM_ERR_ARG;
-    if (!(o.null_frac >= 0))
+    if (!(o.null_frac >= 0) || !(o.refine_kappa >= 0))
         return EM_ERR_ARG;
     if (total_steps > (size_t)INT_MAX || p > (size_t)(INT_MAX / 64) ||
         n > (size_t)(LLONG_MAX / 64) / total_steps)
@@ -200,10 +200,9 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
                                     stage_layout(pl.arith), pl.cfg.tile_recs, s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(c.errbuf, 0, 64, s);
-    // mixed: the largest |q| bounds a single contribution (status word 20)
-    float *qabs = reinterpret_cast<float *>(static_cast<unsigned char *>(c.errbuf) + 20);
-    if (e == cudaSuccess && pl.arith == ARITH_MIXED && p)
-        e = launch_abs_charge_max(static_cast<const float *>(c.charges_raw), (int)p, qabs, s);
+    // mixed: the count of re-evaluated vertices (status word at byte 32)
+    unsigned long long *refines = reinterpret_cast<unsigned long long *>(
+        static_cast<unsigned char *>(c.errbuf) + 32);
     if (e == cudaSuccess && !o.device_ptrs) {
         e = cudaMemcpyAsync(dx, x + line0, nl * sizeof(T), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
@@ -230,8 +229,13 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     prm.rule = use_curvature ? o.rule : RULE_FIXED;
     prm.resolution = resolution;
     prm.err = c.err;
-    prm.qabs = qabs;
-    prm.null_frac = o.null_frac > 0 ? o.null_frac : 1e-4;
+    const double kappa = o.refine_kappa > 0 ? o.refine_kappa : kMixKappaDefault;
+    prm.kappa2 = kappa * kappa;
+    prm.refines = refines;
+    // the mixed form's groups come from a queue (status word at byte 40)
+    if (pl.arith == ARITH_MIXED)
+        prm.group_ctr = reinterpret_cast<unsigned long long *>(
+            static_cast<unsigned char *>(c.errbuf) + 40);
     if (o.field_out) {
         prm.ox = static_cast<T *>(o.field_out);
         prm.oy = prm.ox + n * (total_steps - 1);
@@ -341,7 +345,12 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         return code;
     float ms = 0;
     cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    unsigned long long nref = 0;
+    if (perf && pl.arith == ARITH_MIXED &&
+        cudaMemcpy(&nref, refines, sizeof(nref), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return map_cuda(cudaGetLastError());
     if (perf) {
+        perf->fp64_refines = (double)nref;
         const double tk = ms * 1e-3;
         perf->time = tk;
         perf->pairs = (double)nl * (double)(total_steps - 1) * (double)p;

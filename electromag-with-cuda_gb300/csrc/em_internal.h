@@ -62,12 +62,16 @@ template <class T> struct RefTraceParams {
     // the seeds the SSE rule's curvature reads (null: row 0 of x, y, z); a
     // launch that resumes a trace passes x, y, z from its start row
     const T *seed_x, *seed_y, *seed_z;
-    // mixed arithmetic: largest |q| and the re-evaluation threshold
-    const float *qabs;
-    double null_frac;
+    // mixed arithmetic: the conditioning bound kappa^2 of the re-evaluation
+    // test, and the count of re-evaluated vertices (null: not counted)
+    double kappa2;
+    unsigned long long *refines;
     // optional: the field each step uses (Coulomb constant applied, after
     // any re-evaluation), stored like fx (null: none)
     T *ox, *oy, *oz;
+    // optional (resident charges only): a zeroed counter from which warps
+    // take line groups in order instead of the fixed round-robin deal
+    unsigned long long *group_ctr;
 };
 
 // Extended tracer (em_trace_ext.cu).
@@ -256,8 +260,6 @@ constexpr int kUnroll = 8;
 template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream);
-// Largest |q| of p raw records (FP32 bits, a non-negative float) into *out.
-cudaError_t launch_abs_charge_max(const float *raw, int p, float *out, cudaStream_t stream);
 
 // Stages p raw charge records into p_pad records (pad record {1e15, 1e15,
 // 1e15, 0}, whose contribution is exactly zero), plain (paired = 0) or in

@@ -12,6 +12,11 @@ namespace em {
 
 constexpr int kMaxDevices = 64;
 
+// Mixed arithmetic on the reference-layout tracer: a vertex's field is
+// re-evaluated in double-float where the terms' size, sqrt(sum_j |t_j|^2),
+// exceeds this multiple of |E| (the FP32 sum's error grows with it).
+constexpr double kMixKappaDefault = 2.5;
+
 // Cached per-device state.  `mu` serialises calls on one device; buffers
 // only grow and are released by em_release().
 struct DevCtx {
@@ -59,7 +64,10 @@ struct Plan {
 inline long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
 // Staged charge layout for a kernel arithmetic (stage_kernel's `paired`).
-inline int stage_layout(int arith) { return arith == ARITH_FAST2 ? 1 : 0; }
+inline int stage_layout(int arith)
+{
+    return arith == ARITH_FAST2 || arith == ARITH_MIXED ? 1 : 0;
+}
 
 // Relative cost of one line-group step for `tpl` threads per line and `kl`
 // lines per lane: pair work per lane (one charge load per kl pairs) plus
@@ -161,14 +169,14 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     // lines per lane: searched for the fast scalar form when the caller does
     // not say (two lines share each charge load, one line doubles the warps
     // for small line counts); 2 for packed pairs, 1 for exact arithmetic
-    // (mixed: 1 unless asked; two lines' compensated sums and FP64
-    // positions do not fit the 80 registers of a 768-thread CTA: 1534
-    // against 1731 Gpair/s at 24 warps on 32 736 lines x 4096 charges)
+    // (mixed: 2 unless asked, in CTAs of at most 512 threads, whose 128
+    // registers hold two lines' packed chunk sums, compensated sums and
+    // FP64 positions)
     int fixed_kl = 1;
     if (arith == ARITH_FAST)
         fixed_kl = o.lines_per_thread;
     else if (arith == ARITH_MIXED)
-        fixed_kl = o.lines_per_thread ? o.lines_per_thread : 1;
+        fixed_kl = o.lines_per_thread ? o.lines_per_thread : 2;
     else if (arith == ARITH_FAST2)
         fixed_kl = o.lines_per_thread ? o.lines_per_thread : 2;
     const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
@@ -178,14 +186,14 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     const size_t p_res = (p + gran_max - 1) / gran_max * gran_max;
     const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
     // the mixed form's per-line sums need more than 64 registers: at most
-    // 768 threads (80 registers) per CTA
-    const int max_warps = (arith == ARITH_MIXED ? 24 : 32) - (resident ? 0 : 1);
+    // 512 threads (128 registers) per CTA
+    const int max_warps = (arith == ARITH_MIXED ? 16 : 32) - (resident ? 0 : 1);
     choose_shape((long long)n, (long long)p, c.nsm, max_warps, fixed_tpl, fixed_kl, &tpl, &kl,
                  &warps);
     if (o.warps_per_cta)
         warps = std::min(o.warps_per_cta, max_warps);
     // records per padding granule: every lane gets whole unrolled groups
-    const int gran = tpl * kUnroll * (arith == ARITH_FAST2 ? 2 : 1);
+    const int gran = tpl * kUnroll * (stage_layout(arith) ? 2 : 1);
     Plan r;
     r.arith = arith;
     r.n_groups = ceil_div((long long)n, kl * 32 / tpl);

@@ -151,44 +151,195 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
     }
 }
 
-// Mixed arithmetic (FP32 records only): the pairs of records [0, count) of
-// KL lines for lane t of TPL, the inv^3 Newton correction, compensated
-// every kChunk pairs per lane into each line's (hi, lo) sums; dall gets the
-// nearest distance^2 (the null test's contribution bound).
+// Mixed arithmetic (FP32 records in the paired layout, two charges per
+// packed .f32x2 instruction): the pairs of records [0, count) of KL lines
+// for lane t of TPL.
+//
+// Term.  With y = rsqrt(r2) (relative error d) and w = y*y, the product
+// r2*w = 1 + 2d, and q/|r|^3 = q y^3 (2.5 - 1.5 r2 w) + O(d^2): one Newton
+// correction.  Written as v * (r2 w - 5/3) with v = q y w it costs two
+// operations beyond the plain term and yields -(2/3) q/|r|^3; the factor
+// -3/2 (and the rounding of 5/3 to FP32, a constant factor) goes into the
+// per-vertex scale kMixScale.  14 FMA-pipe operations per pair against the
+// plain term's 12.
+//
+// Sums.  Each lane adds its terms into FP32 chunk sums of kMixChunk charge
+// pairs (both halves folded), which enter compensated (hi, lo) sums; l2
+// collects the squared chunk sums, an estimate of sum_j |t_j|^2 that the
+// per-vertex test compares with |E|^2 (the rounding error of the FP32 sum
+// grows with the size of the terms, not of their sum).
+constexpr int kMixChunk = 32;                       // charge pairs per lane and chunk
+constexpr float kMixC53 = -1.66666663f;             // -5/3 rounded to FP32
+// -(3/2) / ((1 + kMixC53) / (1 - 5/3)): the terms' scale back to q r/|r|^3
+constexpr double kMixScale = -1.5 / ((1.0 + (double)kMixC53) / (1.0 - 5.0 / 3.0));
+
 template <int TPL, int KL>
 __device__ __forceinline__ void accumulate_mixed(const float4 *tile, int count, int t,
                                                  const float *px, const float *py,
                                                  const float *pz, CF *hx, CF *hy, CF *hz,
-                                                 float *dall)
+                                                 float *l2)
 {
-    for (int j0 = t; j0 < count; j0 += TPL * kChunk) {
-        const int j1 = min(count, j0 + TPL * kChunk);
-        float ax[KL], ay[KL], az[KL];
+    const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(tile);
+    const int G = count / 2; // charge pairs: {xa,xb,ya,yb} plane, then {za,zb,qa,qb}
+    const u64 C53 = f2_pack(kMixC53, kMixC53);
+    u64 PX[KL], PY[KL], PZ[KL];
+#pragma unroll
+    for (int k = 0; k < KL; ++k) {
+        PX[k] = f2_pack(px[k], px[k]);
+        PY[k] = f2_pack(py[k], py[k]);
+        PZ[k] = f2_pack(pz[k], pz[k]);
+    }
+    for (int j0 = t; j0 < G; j0 += TPL * kMixChunk) {
+        const int j1 = min(G, j0 + TPL * kMixChunk);
+        u64 AX[KL], AY[KL], AZ[KL];
 #pragma unroll
         for (int k = 0; k < KL; ++k)
-            ax[k] = ay[k] = az[k] = 0.0f;
+            AX[k] = AY[k] = AZ[k] = 0ull;
 #pragma unroll 4
-        for (int j = j0; j < j1; j += TPL) {
-            const float4 c = tile[j];
+        for (int jp = j0; jp < j1; jp += TPL) {
+            const ulonglong2 A = tp[jp], B = tp[G + jp];
 #pragma unroll
             for (int k = 0; k < KL; ++k) {
-                const float dx = px[k] - c.x, dy = py[k] - c.y, dz = pz[k] - c.z;
-                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                dall[k] = fminf(dall[k], r2);
-                const float inv = rsqrt_fast(r2);
-                const float inv2 = inv * inv;
-                const float s0 = (c.w * inv) * inv2;
-                const float sc = s0 * fmaf(-1.5f * r2, inv2, 2.5f);
-                ax[k] = fmaf(sc, dx, ax[k]);
-                ay[k] = fmaf(sc, dy, ay[k]);
-                az[k] = fmaf(sc, dz, az[k]);
+                const u64 dx = f2_sub(PX[k], A.x), dy = f2_sub(PY[k], A.y),
+                          dz = f2_sub(PZ[k], B.x);
+                const u64 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                const u64 y = f2_rsqrt(r2);
+                const u64 w = f2_mul(y, y);
+                const u64 v = f2_mul(f2_mul(B.y, y), w);
+                const u64 sc = f2_mul(v, f2_fma(r2, w, C53));
+                AX[k] = f2_fma(sc, dx, AX[k]);
+                AY[k] = f2_fma(sc, dy, AY[k]);
+                AZ[k] = f2_fma(sc, dz, AZ[k]);
             }
         }
 #pragma unroll
         for (int k = 0; k < KL; ++k) {
-            hx[k].add(ax[k]);
-            hy[k].add(ay[k]);
-            hz[k].add(az[k]);
+            float a, b;
+            f2_unpack(AX[k], a, b);
+            const float sx = a + b;
+            f2_unpack(AY[k], a, b);
+            const float sy = a + b;
+            f2_unpack(AZ[k], a, b);
+            const float sz = a + b;
+            hx[k].add(sx);
+            hy[k].add(sy);
+            hz[k].add(sz);
+            l2[k] = fmaf(sx, sx, fmaf(sy, sy, fmaf(sz, sz, l2[k])));
+        }
+    }
+}
+
+// Double-float field (q r/|r|^3 summed, no Coulomb constant) at an FP32
+// point from the staged paired-layout records in global memory (blocks of
+// `block` records: the block's A plane, then its B plane), computed by the
+// whole warp: lane l takes charge pairs l, l + 32, ...; every lane returns
+// the same sums.
+__device__ __noinline__ void refine_df_warp(const float4 *rec, int p_pad, int block, int lane,
+                                            float px, float py, float pz, double &fx,
+                                            double &fy, double &fz)
+{
+    CF hx, hy, hz;
+    const int half = block / 2;
+    for (int gp = lane; gp < p_pad / 2; gp += 32) {
+        const int b = gp / half, jp = gp - b * half;
+        const float4 A = __ldg(rec + (size_t)b * block + jp);
+        const float4 B = __ldg(rec + (size_t)b * block + half + jp);
+        DF tx, ty, tz;
+        float r2h;
+        df_pair(px, py, pz, make_float4(A.x, A.z, B.x, B.z), tx, ty, tz, r2h);
+        cf_add_df(hx, tx);
+        cf_add_df(hy, ty);
+        cf_add_df(hz, tz);
+        df_pair(px, py, pz, make_float4(A.y, A.w, B.y, B.w), tx, ty, tz, r2h);
+        cf_add_df(hx, tx);
+        cf_add_df(hy, ty);
+        cf_add_df(hz, tz);
+    }
+    fx = group_sum<double, 32>((double)hx.h + (double)hx.l);
+    fy = group_sum<double, 32>((double)hy.h + (double)hy.l);
+    fz = group_sum<double, 32>((double)hz.h + (double)hz.l);
+}
+
+// End of a step in the mixed arithmetic for the KL lines of lane t: the
+// group's compensated sums, scaled back to the field in FP64 and rounded
+// once; the test of the sum's conditioning (sum_j |t_j|^2 > kappa^2 |E|^2,
+// from the chunk sums); the double-float field of every flagged vertex,
+// each computed by the whole warp; the reference's step in FP32 and the
+// position accumulated in FP64.
+template <int TPL, int KL>
+__device__ __forceinline__ void finish_mixed(const RefTraceParams<float> &P, int step, int t,
+                                             int lane, const long long *line, const bool *own,
+                                             float *px, float *py, float *pz, double *qx,
+                                             double *qy, double *qz, CF *hx, CF *hy, CF *hz,
+                                             const float *l2)
+{
+    const size_t n = (size_t)P.n;
+    constexpr double kScale = kMixScale * kElectroK;
+    float ex[KL], ey[KL], ez[KL];
+    bool redo[KL];
+#pragma unroll
+    for (int k = 0; k < KL; ++k) {
+        group_two_sum<TPL>(hx[k]);
+        group_two_sum<TPL>(hy[k]);
+        group_two_sum<TPL>(hz[k]);
+        const float l2s = group_sum<float, TPL>(l2[k]);
+        const double sx = (double)hx[k].h + (double)hx[k].l;
+        const double sy = (double)hy[k].h + (double)hy[k].l;
+        const double sz = (double)hz[k].h + (double)hz[k].l;
+        redo[k] = own[k] && (double)l2s > P.kappa2 * (sx * sx + sy * sy + sz * sz);
+        ex[k] = (float)(sx * kScale);
+        ey[k] = (float)(sy * kScale);
+        ez[k] = (float)(sz * kScale);
+    }
+#pragma unroll
+    for (int k = 0; k < KL; ++k) {
+        unsigned m = __ballot_sync(0xffffffffu, redo[k] && t == 0);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const float rx = __shfl_sync(0xffffffffu, px[k], src);
+            const float ry = __shfl_sync(0xffffffffu, py[k], src);
+            const float rz = __shfl_sync(0xffffffffu, pz[k], src);
+            double fx, fy, fz;
+            refine_df_warp(static_cast<const float4 *>(P.charges), P.p_pad, P.tile_recs, lane,
+                           rx, ry, rz, fx, fy, fz);
+            if (lane / TPL == src / TPL) {
+                ex[k] = (float)(fx * kElectroK);
+                ey[k] = (float)(fy * kElectroK);
+                ez[k] = (float)(fz * kElectroK);
+            }
+            if (lane == src && P.refines)
+                atomicAdd(P.refines, 1ull);
+        }
+    }
+    const bool curvature = P.rule != RULE_FIXED;
+#pragma unroll
+    for (int k = 0; k < KL; ++k) {
+        if (P.ox && own[k] && t == 0) {
+            const size_t fi = (size_t)(step - 1) * n + (size_t)line[k];
+            store_stream(P.ox + fi, ex[k]);
+            store_stream(P.oy + fi, ey[k]);
+            store_stream(P.oz + fi, ez[k]);
+        }
+        float r0x = px[k], r0y = py[k], r0z = pz[k];
+        if (P.rule == RULE_SSE && own[k]) {
+            r0x = ld_seed(P.seed_x + line[k]);
+            r0y = ld_seed(P.seed_y + line[k]);
+            r0z = ld_seed(P.seed_z + line[k]);
+        }
+        float sx, sy, sz;
+        step_of<float>(ex[k], ey[k], ez[k], r0x, r0y, r0z, curvature, P.resolution, sx, sy, sz);
+        qx[k] += (double)sx;
+        qy[k] += (double)sy;
+        qz[k] += (double)sz;
+        px[k] = (float)qx[k];
+        py[k] = (float)qy[k];
+        pz[k] = (float)qz[k];
+        if (own[k] && t == 0) {
+            const size_t idx = (size_t)step * n + (size_t)line[k];
+            store_stream(P.x + idx, px[k]);
+            store_stream(P.y + idx, py[k]);
+            store_stream(P.z + idx, pz[k]);
         }
     }
 }
@@ -277,11 +428,22 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
     }
 
     // ---- compute warps --------------------------------------------------------
+    // Groups: dealt round-robin to CTAs, or, with resident charges and a
+    // group counter (the mixed form, whose re-evaluations make some groups
+    // slower than others), taken one at a time by whichever warp is free.
+    const bool queued = !streamed && P.group_ctr;
     uint32_t it = 0;
-    for (int r = 0; r < rounds; ++r) {
-        const long long gk = (long long)r * ncw + warp;
-        const long long g = blockIdx.x + (long long)gridDim.x * gk;
-        const bool active = gk < cta_groups;
+    for (int r = 0; queued || r < rounds; ++r) {
+        long long gk = (long long)r * ncw + warp;
+        long long g = blockIdx.x + (long long)gridDim.x * gk;
+        bool active = gk < cta_groups;
+        if (queued) {
+            unsigned long long q = 0;
+            if (lane == 0)
+                q = atomicAdd(P.group_ctr, 1ull);
+            g = (long long)__shfl_sync(0xffffffffu, q, 0);
+            active = g < P.n_groups;
+        }
         if (!streamed && !active)
             break;
         long long line[KL];
@@ -306,17 +468,17 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
         for (int step = 1; step < P.total_steps; ++step) {
             Acc<T> acc[KL];
             CF hx[KL], hy[KL], hz[KL];
-            float dall[KL];
+            float l2[KL];
 #pragma unroll
             for (int k = 0; k < KL; ++k)
-                dall[k] = 3.0e38f;
+                l2[k] = 0.0f;
             auto charges_of = [&](const Rec *tp, int count) {
                 if constexpr (ARITH == ARITH_MIXED)
                     accumulate_mixed<TPL, KL>(reinterpret_cast<const float4 *>(tp), count, t,
                                               reinterpret_cast<const float *>(px),
                                               reinterpret_cast<const float *>(py),
                                               reinterpret_cast<const float *>(pz), hx, hy, hz,
-                                              dall);
+                                              l2);
                 else
                     accumulate_k<T, TPL, ARITH, KL>(tp, count, t, px, py, pz, K, three_arg,
                                                     acc);
@@ -337,18 +499,16 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                 if (!active)
                     continue;
             }
+            if constexpr (ARITH == ARITH_MIXED) {
+                finish_mixed<TPL, KL>(P, step, t, lane, line, own, px, py, pz, qx, qy, qz, hx,
+                                      hy, hz, l2);
+                continue;
+            }
 #pragma unroll
             for (int k = 0; k < KL; ++k) {
                 acc_finish<T, ARITH>(acc[k]);
                 T ax = acc[k].x, ay = acc[k].y, az = acc[k].z;
-                if constexpr (ARITH == ARITH_MIXED) {
-                    group_two_sum<TPL>(hx[k]);
-                    group_two_sum<TPL>(hy[k]);
-                    group_two_sum<TPL>(hz[k]);
-                    ax = (T)__fadd_rn(hx[k].h, hx[k].l);
-                    ay = (T)__fadd_rn(hy[k].h, hy[k].l);
-                    az = (T)__fadd_rn(hz[k].h, hz[k].l);
-                } else if (TPL > 1) {
+                if (TPL > 1) {
                     ax = line_reduce<T, TPL>(ax);
                     ay = line_reduce<T, TPL>(ay);
                     az = line_reduce<T, TPL>(az);
@@ -375,50 +535,14 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                     r0y = ld_seed(P.seed_y + line[k]);
                     r0z = ld_seed(P.seed_z + line[k]);
                 }
-                if constexpr (ARITH == ARITH_MIXED) {
-                    // near a null |E| is far below its largest term and the
-                    // FP32 sum loses its digits: the field again in FP64
-                    const float dmin = group_min<float, TPL>(dall[k]);
-                    const float bound = *P.qabs * (float)kElectroK / dmin;
-                    const float e2 = (float)(ax * ax + ay * ay + az * az);
-                    const float lim2 = (float)P.null_frac * bound;
-                    const bool redo = own[k] && !(e2 >= lim2 * lim2);
-                    if (__any_sync(0xffffffffu, redo)) {
-                        double fx = 0, fy = 0, fz = 0;
-                        if (redo)
-                            field_fp64<TPL>(static_cast<const float4 *>(P.charges), P.p_pad, t,
-                                            (double)px[k], (double)py[k], (double)pz[k], fx,
-                                            fy, fz);
-                        fx = group_sum<double, TPL>(fx);
-                        fy = group_sum<double, TPL>(fy);
-                        fz = group_sum<double, TPL>(fz);
-                        if (redo) {
-                            ax = (T)(fx * kElectroK);
-                            ay = (T)(fy * kElectroK);
-                            az = (T)(fz * kElectroK);
-                        }
-                    }
-                }
                 if (P.ox && own[k] && t == 0) {
                     const size_t fi = (size_t)(step - 1) * n + (size_t)line[k];
                     store_stream(P.ox + fi, ax);
                     store_stream(P.oy + fi, ay);
                     store_stream(P.oz + fi, az);
                 }
-                if constexpr (ARITH == ARITH_MIXED) {
-                    // the reference's step in FP32, the position in FP64
-                    T sx, sy, sz;
-                    step_of<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, sx, sy, sz);
-                    qx[k] += (double)sx;
-                    qy[k] += (double)sy;
-                    qz[k] += (double)sz;
-                    px[k] = (T)qx[k];
-                    py[k] = (T)qy[k];
-                    pz[k] = (T)qz[k];
-                } else {
-                    advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k],
-                               py[k], pz[k]);
-                }
+                advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k], py[k],
+                           pz[k]);
                 if (own[k] && t == 0) {
                     const size_t idx = (size_t)step * n + (size_t)line[k];
                     store_stream(P.x + idx, px[k]);
@@ -494,15 +618,13 @@ cudaError_t launch_fast(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaSt
                           : launch_one<T, TPL, ARITH_FAST, 1, 1024>(p, cfg, stream);
 }
 
+// Mixed form: up to 512 threads per CTA (128 registers: two lines' packed
+// chunk sums, compensated sums and FP64 positions).
 template <class T, int TPL>
 cudaError_t launch_mixed(const RefTraceParams<T> &p, const LaunchCfg &cfg, cudaStream_t stream)
 {
-    const int threads = 32 * (cfg.warps + (cfg.resident ? 0 : 1));
-    if (cfg.kl == 2)
-        return threads <= 768 ? launch_one<T, TPL, ARITH_MIXED, 2, 768>(p, cfg, stream)
-                              : launch_one<T, TPL, ARITH_MIXED, 2, 1024>(p, cfg, stream);
-    return threads <= 768 ? launch_one<T, TPL, ARITH_MIXED, 1, 768>(p, cfg, stream)
-                          : launch_one<T, TPL, ARITH_MIXED, 1, 1024>(p, cfg, stream);
+    return cfg.kl == 2 ? launch_one<T, TPL, ARITH_MIXED, 2, 512>(p, cfg, stream)
+                       : launch_one<T, TPL, ARITH_MIXED, 1, 512>(p, cfg, stream);
 }
 
 template <class T, int TPL>
@@ -574,38 +696,6 @@ cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad
         return cudaErrorInvalidValue;
     stage_kernel<T><<<(p_pad + 127) / 128, 128, 0, stream>>>(
         static_cast<const T *>(raw), p, static_cast<T *>(staged), p_pad, paired, block);
-    count_launch(1);
-    return cudaGetLastError();
-}
-
-namespace {
-
-// Largest |q| over p records, one CTA of 256 (a warp maximum per warp, then
-// the CTA's).
-__global__ void __launch_bounds__(256) abs_charge_max_kernel(const float *raw, int p, float *out)
-{
-    __shared__ float wm[8];
-    float m = 0;
-    for (int i = threadIdx.x; i < p; i += blockDim.x)
-        m = fmaxf(m, fabsf(raw[4 * (size_t)i + 3]));
-    for (int o = 16; o; o >>= 1)
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0)
-        wm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-            r = fmaxf(r, wm[w]);
-        *out = r;
-    }
-}
-
-} // namespace
-
-cudaError_t launch_abs_charge_max(const float *raw, int p, float *out, cudaStream_t stream)
-{
-    abs_charge_max_kernel<<<1, 256, 0, stream>>>(raw, p, out);
     count_launch(1);
     return cudaGetLastError();
 }

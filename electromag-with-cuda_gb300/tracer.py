@@ -49,13 +49,14 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                arith="fast", rule="sse", require_n64=None, stream=None,
                threads_per_line=0, warps_per_cta=0, tile_charges=0,
                force_streamed=False, pack="auto", lines_per_thread=0,
-               plain=None, null_frac=0.0, field_out=None):
+               plain=None, null_frac=0.0, field_out=None, refine_kappa=0.0):
     """Traces n field lines in place; returns (rc, perf).
 
     arith: "fast" (FP32/FP64 rsqrt + FMA), "exact" (the reference's IEEE
     sequence) or "mixed" (float32 only: compensated FP32 pairs with a
     Newton-corrected inv^3, the position in FP64, the field re-evaluated in
-    FP64 below null_frac (default 1e-4) of the largest contribution).
+    double-float where sqrt(sum |t_j|^2) exceeds refine_kappa (default
+    2.5) times |E|).
 
     rc is the reference's code (0 ok, 1 n == 0, 2 resolution == 0,
     3 total_steps < 2, 5 n % 64 with require_n64) or a library code >= 4.
@@ -80,7 +81,8 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
                  and require_n64 in (None, True) and not threads_per_line
                  and not warps_per_cta and not tile_charges
                  and not force_streamed and pack == "auto"
-                 and not lines_per_thread and field_out is None)
+                 and not lines_per_thread and field_out is None
+                 and not refine_kappa)
     if plain:
         if device:
             raise ValueError("the plain entry point takes host arrays")
@@ -105,6 +107,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     o.pack = _PACK[pack]
     o.lines_per_thread = lines_per_thread
     o.null_frac = null_frac
+    o.refine_kappa = refine_kappa
     if field_out is not None:
         if not (_is_torch(field_out) and field_out.is_cuda and device):
             raise ValueError("field_out needs CUDA tensors throughout")

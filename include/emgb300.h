@@ -58,12 +58,12 @@ extern "C" {
 #define EM_ARITH_FAST 0   /* FP32 (or FP64 for _f64) rsqrt + FMA             */
 #define EM_ARITH_EXACT 1  /* the reference's IEEE operation sequence:
                              bit-identical to its strict x86 build          */
-#define EM_ARITH_MIXED 2  /* _f32 only: FP32 pairs with a Newton-corrected
-                             inv^3, compensated sums, the line position in
-                             FP64, the field re-evaluated in FP64 where |E|
-                             is below null_frac of the largest single
-                             contribution (the extended tracer's
-                             EM_PREC_MIXED, on the reference's loop)        */
+#define EM_ARITH_MIXED 2  /* _f32 only: FP32 pairs (two charges per packed
+                             instruction) with a Newton-corrected inv^3,
+                             compensated chunk sums, the line position in
+                             FP64, and the field re-evaluated in
+                             double-float where the sum is ill-conditioned
+                             (sqrt(sum |t_j|^2) > refine_kappa |E|)        */
 
 /* ---- stepping rule (which reference routine to reproduce) ---------------- */
 #define EM_RULE_SSE 0      /* CalcField_CPU_T_Curvature<float/double> SSE
@@ -81,7 +81,8 @@ typedef struct em_perf {
     volatile double progress; /* 0 before the call, 1.0 when complete        */
     double pairs;        /* pair interactions evaluated                      */
     double wall_time;    /* seconds of the whole call (copies included)      */
-    double fp64_refines; /* vertices whose field was redone in FP64 (mixed)  */
+    double fp64_refines; /* vertices whose field was re-evaluated at higher
+                            precision (mixed arithmetic)                     */
 } em_perf;
 
 /* Options for the _ex entry points.  Zero-initialise and set what you need. */
@@ -123,6 +124,11 @@ typedef struct em_options {
                              arrays of n*(total_steps-1) values back to back
                              (x, then y, then z), the field at vertex s of
                              line l at s*n + l                               */
+    double refine_kappa;  /* EM_ARITH_MIXED, em_calc_field_ex_f32: a vertex's
+                             field is re-evaluated in double-float where the
+                             terms' size sqrt(sum_j |t_j|^2) (estimated from
+                             the compensated chunk sums) exceeds
+                             refine_kappa * |E| (0: 2.5)                     */
 } em_options;
 
 /* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
