@@ -42,17 +42,14 @@ int main()
     o.arith = EM_ARITH_EXACT;
     expect("exact", make_plan<float>(c, 16384, 1024, o, &p) == EM_OK && p.cfg.tpl == 1 &&
                         p.cfg.kl == 1 && p.arith == ARITH_EXACT);
-    // mixed: one line per lane, at most 24 warps (768-thread CTAs); on the
-    // gpu-scale set 20 warps, whose third round keeps 14 of 54 groups per SM
-    // busy (measured 1792-1794 Gpair/s against 1727-1731 at 24 warps, whose third
-    // round runs 6)
+    // mixed: 8 lanes x 2 lines, every warp of a 512-thread CTA the groups
+    // keep busy (groups come from a queue: no round balancing)
     o.arith = EM_ARITH_MIXED;
     expect("mixed", make_plan<float>(c, 32736, 4096, o, &p) == EM_OK && p.cfg.tpl == 8 &&
-                        p.cfg.kl == 1 && p.cfg.warps == 20 && p.arith == ARITH_MIXED);
-    // 16 384 lines x 1024 charges: the same 20 warps (1415 Gpair/s against
-    // 1345 at 24)
+                        p.cfg.kl == 2 && p.cfg.warps == 16 && p.arith == ARITH_MIXED);
+    // 16 384 lines: 2048 groups, 14 per SM
     expect("mixed 16384x1024", make_plan<float>(c, 16384, 1024, o, &p) == EM_OK &&
-                                   p.cfg.tpl == 8 && p.cfg.kl == 1 && p.cfg.warps == 20);
+                                   p.cfg.tpl == 8 && p.cfg.kl == 2 && p.cfg.warps == 14);
     expect("mixed fp64 rejected", make_plan<double>(c, 32736, 4096, o, &p) == EM_ERR_ARG);
     o.arith = EM_ARITH_FAST;
     // 20 000 charges do not fit: streamed tiles, a producer warp's room left
