@@ -376,8 +376,15 @@ def main():
         e2e = run_e2e(em, torch, dist, ch, seeds, rows, args, world)
 
     extras = {}
+    field_err = None
     if not args.no_extras and world == 1:
-        extras = run_extras(em, torch, dev, args)
+        # the timed path's own field at sampled vertices of one more
+        # (untimed) trace of the same workload and shape
+        del X
+        torch.cuda.empty_cache()
+        _, field_err = traced_field_errors(em, torch, dev, ch, seeds, rows,
+                                           20000, args.seed + 1, **shape)
+        extras = run_extras(em, torch, dev, args, value)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -410,44 +417,83 @@ def main():
                      "achieved_reference_convention":
                          (18.0 * pairs + 13.0 * n * (rows - 1)) / kernel_s / 1e12,
                      "kernel_ms": kernel_s * 1e3},
+        "field_err": field_err,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
     line.update(extras)
-    line["metric_parts"] = metric_parts(value, extras)
+    line["metric_parts"] = metric_parts(value, extras, field_err)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
 
 
-def metric_parts(value, extras):
-    """The metric's parts in one place: the plain FP32 rate (`value`), the
-    extended tracer's mixed mode per pair (200 rows, no termination) against
-    it and against the extended tracer's own FP32 form (the same lane-group
-    kernel, the per-pair cost of the mixed arithmetic alone), its field
-    error vs FP64, the mixed arithmetic on the reference-layout tracer (the
-    same loop as `value`) against `value`, and the adjoint/forward time
-    ratio."""
+def fastest_within(candidates, bound=1e-6):
+    """The fastest (name, rate, max error) candidate whose sampled maximum
+    field error is within `bound`, or None."""
+    ok = [c for c in candidates if c[1] and c[2] is not None and c[2] <= bound]
+    if not ok:
+        return None
+    name, rate, err = max(ok, key=lambda c: c[1])
+    return {"mode": name, "gpair_s": rate, "field_err_max": err}
+
+
+def metric_parts(value, extras, value_err=None):
+    """The metric's parts in one place: the plain FP32 rate (`value`) and
+    its field error; the mixed arithmetic on the reference-layout tracer
+    (the same loop and workload as `value`) against `value`, with its field
+    error; the extended tracer's mixed mode per pair (200 rows, no
+    termination) against `value` and against the extended tracer's own FP32
+    form; the fastest mode whose maximum sampled field error is within 1e-6
+    of FP64 on the GPU-scale and the dipole workloads; the adjoint/forward
+    time ratio."""
     parts = {"plain_fp32_gpair_s": value}
+    if value_err:
+        parts["plain_fp32_field_err_max"] = value_err["vs_fp64"]["max"]
+    mref = extras.get("mixed_reference_layout", {})
+    if "gpair_s" in mref:
+        e = mref["field_err"]["vs_fp64"]
+        parts.update({"mixed_reference_layout_gpair_s": mref["gpair_s"],
+                      "mixed_reference_layout_vs_plain_fp32": mref["gpair_s"] / value,
+                      "mixed_reference_layout_field_err_median": e["median"],
+                      "mixed_reference_layout_field_err_max": e["max"],
+                      "mixed_reference_layout_frac_le_1e-6": e["frac_le_1e-6"],
+                      "mixed_reference_layout_refined_vertex_frac":
+                          mref["refined_vertex_frac"]})
     prec = extras.get("precision", {})
     if "mixed_vs_fp32" in prec:
         mixed = prec.get("mixed", {}).get("field_err_vs_fp64") or {}
         rates = prec.get("no_termination_200_rows_gpair_s", {})
-        parts.update({"mixed_gpair_s": rates.get("mixed"),
-                      "mixed_vs_plain_fp32": (rates["mixed"] / value
-                                              if rates.get("mixed") else None),
-                      "mixed_vs_extended_fp32": prec["mixed_vs_fp32"],
-                      "mixed_vs_fp64": prec.get("mixed_vs_fp64"),
-                      "mixed_field_err_median": mixed.get("median"),
-                      "mixed_field_err_max": mixed.get("max"),
-                      "mixed_frac_le_1e-6": mixed.get("frac_le_1e-6")})
-    mref = extras.get("mixed_reference_layout", {})
-    if "gpair_s" in mref:
-        parts["mixed_reference_layout_gpair_s"] = mref["gpair_s"]
-        parts["mixed_reference_layout_vs_plain_fp32"] = mref["gpair_s"] / value
+        parts.update({"extended_mixed_gpair_s": rates.get("mixed"),
+                      "extended_mixed_vs_plain_fp32": (rates["mixed"] / value
+                                                       if rates.get("mixed") else None),
+                      "extended_mixed_vs_extended_fp32": prec["mixed_vs_fp32"],
+                      "extended_mixed_vs_fp64": prec.get("mixed_vs_fp64"),
+                      "extended_mixed_field_err_median": mixed.get("median"),
+                      "extended_mixed_field_err_max": mixed.get("max"),
+                      "extended_mixed_frac_le_1e-6": mixed.get("frac_le_1e-6")})
+    fastest = {}
+    for wl, blk in (("gpu_4096", prec), ("dipole_16384", extras.get("precision_stress", {}))):
+        cands = []
+        if wl == "gpu_4096":
+            if value_err:
+                cands.append(("reference-layout fp32", value, value_err["vs_fp64"]["max"]))
+            if "gpair_s" in mref:
+                cands.append(("reference-layout mixed", mref["gpair_s"],
+                              mref["field_err"]["vs_fp64"]["max"]))
+        for mode in ("fp32", "mixed", "mixed_nf0.05", "mixed_nf0.05_df64", "df64", "fp64"):
+            m = blk.get(mode) or {}
+            err = (m.get("field_err_vs_fp64") or {}).get("max")
+            if m.get("gpair_s"):
+                cands.append(("extended " + mode + " (termination)", m["gpair_s"], err))
+        best = fastest_within(cands)
+        if best:
+            best["vs_plain_fp32"] = best["gpair_s"] / value
+        fastest[wl] = best
+    parts["fastest_mode_max_err_le_1e-6"] = fastest
     adj = extras.get("adjoint", {})
     if "stored" in adj:
         parts["adjoint_over_forward"] = adj["stored"]["adjoint_over_forward"]
@@ -761,40 +807,132 @@ def nbody_functor_block(em, torch, dev, seed):
     return blk
 
 
-def mixed_reference_block(em, torch, dev, args):
+def traced_field_errors(em, torch, dev, ch, seeds, rows, samples, seed,
+                        **kw):
+    """One untimed trace of the reference-layout tracer with its field
+    output, then the field each step used at `samples` vertices (every row
+    and line equally likely) against the FP64 field at the same points
+    (em_field_f64, the reference's double sequence) and against the
+    reference's FP32 field there (em_field_f32 in the exact arithmetic: the
+    reference's own operation sequence, bit for bit)."""
+    n = len(seeds)
+    X = [torch.zeros(n * rows, dtype=torch.float32, device=dev) for _ in range(3)]
+    for c in range(3):
+        X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c])).to(dev)
+    F = torch.zeros(3 * n * (rows - 1), dtype=torch.float32, device=dev)
+    dch = torch.from_numpy(np.ascontiguousarray(ch)).to(dev)
+    rc, perf = em.calc_field(*X, dch, n, 1.0, True, require_n64=False,
+                             field_out=F, **kw)
+    if rc:
+        raise em.EmError(rc, "em_calc_field_ex_f32 (field output)")
+    torch.cuda.synchronize()
+    g = np.random.Generator(np.random.PCG64(seed))
+    li = torch.from_numpy(g.integers(0, n, samples)).to(dev)
+    ri = torch.from_numpy(g.integers(0, rows - 1, samples)).to(dev)
+    pts = torch.stack([x.view(rows, n)[ri, li] for x in X])
+    got = F.view(3, rows - 1, n)[:, ri, li].double()
+    del X, F
+    ref64 = em.field(pts.double().contiguous(), dch.double().contiguous(),
+                     arith="exact")
+    ref32 = em.field(pts.contiguous(), dch, arith="exact", rule="sse").double()
+    out = {}
+    for key, ref in (("vs_fp64", ref64), ("vs_reference_fp32", ref32)):
+        e = ((got - ref).norm(dim=0) / ref.norm(dim=0)).cpu().numpy()
+        out[key] = {"median": float(np.median(e)),
+                    "p99": float(np.quantile(e, 0.99)),
+                    "p999": float(np.quantile(e, 0.999)),
+                    "max": float(e.max()),
+                    "frac_le_1e-6": float((e <= 1e-6).mean()),
+                    "samples": int(samples)}
+    torch.cuda.empty_cache()
+    return perf, out
+
+
+def mixed_reference_block(em, torch, dev, args, value):
     """The mixed arithmetic on the reference-layout tracer (EM_ARITH_MIXED):
     the `value` workload and loop (every line all rows, device arrays), so
-    its rate divides by `value` directly."""
+    its rate divides by `value` directly; its field error at sampled
+    vertices, and the share of vertices re-evaluated in double-float."""
     ch, seeds, rows = workload(em, args.workload, args.seed + 0, args.rows)
     n, p = len(seeds), len(ch)
     X = [torch.zeros(n * rows, dtype=torch.float32, device=dev) for _ in range(3)]
     for c in range(3):
         X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c])).to(dev)
     dch = torch.from_numpy(ch).to(dev)
-    times = []
-    for i in range(3):
+    times, refines = [], 0.0
+    for i in range(4):
         rc, perf = em.calc_field(*X, dch, n, 1.0, True, require_n64=False,
                                  arith="mixed")
         if rc:
             raise em.EmError(rc, "em_calc_field_ex_f32 (mixed)")
         if i:
             times.append(perf.time)
+            refines = perf.fp64_refines
     torch.cuda.synchronize()
+    del X
+    torch.cuda.empty_cache()
     t = float(np.mean(times))
     pairs = float(n) * (rows - 1) * p
+    _, errs = traced_field_errors(em, torch, dev, ch, seeds, rows, 20000,
+                                  args.seed + 1, arith="mixed")
     return {"workload": args.workload, "lines": n, "charges": p, "rows": rows,
-            "ms": t * 1e3, "gpair_s": pairs / t / 1e9}
+            "ms": t * 1e3, "gpair_s": pairs / t / 1e9,
+            "vs_plain_fp32": pairs / t / 1e9 / value,
+            "refined_vertex_frac": refines / (float(n) * (rows - 1)),
+            "field_err": errs}
 
 
-def run_extras(em, torch, dev, args):
+def cpu_config_block(em, torch, dev, seed):
+    """The CPU-runnable configuration (256 charges in [-50,50]^3, 8 seeds
+    per positive charge, 2500 rows) timed whole: the GPU in the fast and the
+    reference's exact arithmetic, and the oracle port of the reference's
+    CPU path over all host cores (the whole run, no sampling)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import em_oracle as orc
+    ch, seeds, rows = workload(em, "cpu_256", seed, None)
+    seeds = em.workloads.pad_lines(seeds, 64)  # the SSE path's n % 64
+    n, p = len(seeds), len(ch)
+    pairs = float(n) * (rows - 1) * p
+    blk = {"workload": "cpu_256", "lines": n, "charges": p, "rows": rows}
+    dch = torch.from_numpy(ch).to(dev)
+    for arith in ("fast", "exact"):
+        best = None
+        for _ in range(3):
+            V = torch.zeros((3, rows, n), dtype=torch.float32, device=dev)
+            V[:, 0, :] = torch.from_numpy(seeds.T.copy()).to(dev)
+            rc, perf = em.calc_field(V[0].reshape(-1), V[1].reshape(-1),
+                                     V[2].reshape(-1), dch, n, 1.0, True,
+                                     arith=arith)
+            if rc:
+                raise em.EmError(rc, f"cpu_256 ({arith})")
+            best = perf.time if best is None else min(best, perf.time)
+        blk["gpu_" + arith] = {"ms": best * 1e3, "gpair_s": pairs / best / 1e9}
+    threads = os.cpu_count() or 1
+    X = [np.zeros(n * rows, np.float32) for _ in range(3)]
+    for c in range(3):
+        X[c][:n] = seeds[:, c]
+    t = time.perf_counter()
+    rc = orc.calc_field(*X, ch, n, 1.0, orc.CURV_SSE, nthreads=threads)
+    sec = time.perf_counter() - t
+    if rc:
+        raise RuntimeError(f"oracle port returned {rc}")
+    blk["cpu_port"] = {"seconds": sec, "gpair_s": pairs / sec / 1e9,
+                       "cores": threads, "sample": "the whole run"}
+    blk["gpu_fast_vs_cpu_port"] = blk["gpu_fast"]["gpair_s"] / blk["cpu_port"]["gpair_s"]
+    return blk
+
+
+def run_extras(em, torch, dev, args, value):
     """Single-GPU measurements of the other configurations; a block that
     fails is reported in its place and does not cost the bench line."""
     blocks = [
+        ("cpu_config", lambda: cpu_config_block(em, torch, dev, args.seed)),
         ("reference_run", lambda: reference_run_block(em, torch, dev, args.seed)),
         ("batched", lambda: batch_block(em, torch, dev, args.seed)),
         ("precision", lambda: precision_block(em, torch, dev, args.workload,
                                               5000, args.seed, 20000, True)),
-        ("mixed_reference_layout", lambda: mixed_reference_block(em, torch, dev, args)),
+        ("mixed_reference_layout", lambda: mixed_reference_block(em, torch, dev, args,
+                                                                 value)),
         ("precision_stress", lambda: precision_block(
             em, torch, dev, "dipole_16384", 4000, args.seed, 20000, False)),
         ("adjoint", lambda: adjoint_block(em, torch, dev, args.seed)),

@@ -164,10 +164,13 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
 // plain term's 12.
 //
 // Sums.  Each lane adds its terms into FP32 chunk sums of kMixChunk charge
-// pairs (both halves folded), which enter compensated (hi, lo) sums; l2
-// collects the squared chunk sums, an estimate of sum_j |t_j|^2 that the
-// per-vertex test compares with |E|^2 (the rounding error of the FP32 sum
-// grows with the size of the terms, not of their sum).
+// pairs (both halves folded), which enter compensated (hi, lo) sums.  l2
+// collects sum_j |t_j|^2 = sum_j q_j^2 y_j^4 (one more packed FMA per
+// charge pair, from q y and v), which the per-vertex test compares with
+// |E|^2: the rounding error of the FP32 sum grows with the size of the
+// terms, not of their sum.  (Squared chunk sums would cost less but miss
+// terms that cancel inside a chunk, such as the two charges of a dipole
+// stored side by side.)
 constexpr int kMixChunk = 32;                       // charge pairs per lane and chunk
 constexpr float kMixC53 = -1.66666663f;             // -5/3 rounded to FP32
 // -(3/2) / ((1 + kMixC53) / (1 - 5/3)): the terms' scale back to q r/|r|^3
@@ -182,12 +185,13 @@ __device__ __forceinline__ void accumulate_mixed(const float4 *tile, int count, 
     const ulonglong2 *tp = reinterpret_cast<const ulonglong2 *>(tile);
     const int G = count / 2; // charge pairs: {xa,xb,ya,yb} plane, then {za,zb,qa,qb}
     const u64 C53 = f2_pack(kMixC53, kMixC53);
-    u64 PX[KL], PY[KL], PZ[KL];
+    u64 PX[KL], PY[KL], PZ[KL], L2[KL];
 #pragma unroll
     for (int k = 0; k < KL; ++k) {
         PX[k] = f2_pack(px[k], px[k]);
         PY[k] = f2_pack(py[k], py[k]);
         PZ[k] = f2_pack(pz[k], pz[k]);
+        L2[k] = 0ull;
     }
     for (int j0 = t; j0 < G; j0 += TPL * kMixChunk) {
         const int j1 = min(G, j0 + TPL * kMixChunk);
@@ -205,11 +209,13 @@ __device__ __forceinline__ void accumulate_mixed(const float4 *tile, int count, 
                 const u64 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
                 const u64 y = f2_rsqrt(r2);
                 const u64 w = f2_mul(y, y);
-                const u64 v = f2_mul(f2_mul(B.y, y), w);
+                const u64 qy = f2_mul(B.y, y);
+                const u64 v = f2_mul(qy, w);
                 const u64 sc = f2_mul(v, f2_fma(r2, w, C53));
                 AX[k] = f2_fma(sc, dx, AX[k]);
                 AY[k] = f2_fma(sc, dy, AY[k]);
                 AZ[k] = f2_fma(sc, dz, AZ[k]);
+                L2[k] = f2_fma(qy, v, L2[k]);
             }
         }
 #pragma unroll
@@ -224,26 +230,29 @@ __device__ __forceinline__ void accumulate_mixed(const float4 *tile, int count, 
             hx[k].add(sx);
             hy[k].add(sy);
             hz[k].add(sz);
-            l2[k] = fmaf(sx, sx, fmaf(sy, sy, fmaf(sz, sz, l2[k])));
         }
+    }
+#pragma unroll
+    for (int k = 0; k < KL; ++k) {
+        float a, b;
+        f2_unpack(L2[k], a, b);
+        l2[k] += a + b;
     }
 }
 
 // Double-float field (q r/|r|^3 summed, no Coulomb constant) at an FP32
-// point from the staged paired-layout records in global memory (blocks of
-// `block` records: the block's A plane, then its B plane), computed by the
-// whole warp: lane l takes charge pairs l, l + 32, ...; every lane returns
-// the same sums.
+// point from staged paired-layout records (blocks of `block` records: the
+// block's A plane, then its B plane) in shared memory (resident charges) or
+// global memory (streamed), computed by the whole warp: lane l takes charge
+// pairs l, l + 32, ..., two per iteration with both loads issued first;
+// every lane returns the same sums.
 __device__ __noinline__ void refine_df_warp(const float4 *rec, int p_pad, int block, int lane,
                                             float px, float py, float pz, double &fx,
                                             double &fy, double &fz)
 {
     CF hx, hy, hz;
-    const int half = block / 2;
-    for (int gp = lane; gp < p_pad / 2; gp += 32) {
-        const int b = gp / half, jp = gp - b * half;
-        const float4 A = __ldg(rec + (size_t)b * block + jp);
-        const float4 B = __ldg(rec + (size_t)b * block + half + jp);
+    const int half = block / 2, npair = p_pad / 2;
+    auto add = [&](const float4 &A, const float4 &B) {
         DF tx, ty, tz;
         float r2h;
         df_pair(px, py, pz, make_float4(A.x, A.z, B.x, B.z), tx, ty, tz, r2h);
@@ -254,6 +263,24 @@ __device__ __noinline__ void refine_df_warp(const float4 *rec, int p_pad, int bl
         cf_add_df(hx, tx);
         cf_add_df(hy, ty);
         cf_add_df(hz, tz);
+    };
+    auto at = [&](int gp, float4 &A, float4 &B) {
+        const int b = gp / half, jp = gp - b * half;
+        A = rec[(size_t)b * block + jp];
+        B = rec[(size_t)b * block + half + jp];
+    };
+    int gp = lane;
+    for (; gp + 32 < npair; gp += 64) {
+        float4 A0, B0, A1, B1;
+        at(gp, A0, B0);
+        at(gp + 32, A1, B1);
+        add(A0, B0);
+        add(A1, B1);
+    }
+    if (gp < npair) {
+        float4 A0, B0;
+        at(gp, A0, B0);
+        add(A0, B0);
     }
     fx = group_sum<double, 32>((double)hx.h + (double)hx.l);
     fy = group_sum<double, 32>((double)hy.h + (double)hy.l);
@@ -267,14 +294,21 @@ __device__ __noinline__ void refine_df_warp(const float4 *rec, int p_pad, int bl
 // each computed by the whole warp; the reference's step in FP32 and the
 // position accumulated in FP64.
 template <int TPL, int KL>
-__device__ __forceinline__ void finish_mixed(const RefTraceParams<float> &P, int step, int t,
+__device__ __forceinline__ void finish_mixed(const RefTraceParams<float> &P,
+                                             const float4 *rec, int step, int t,
                                              int lane, const long long *line, const bool *own,
                                              float *px, float *py, float *pz, double *qx,
                                              double *qy, double *qz, CF *hx, CF *hy, CF *hz,
                                              const float *l2)
 {
     const size_t n = (size_t)P.n;
+    // the scale back to the field (kMixScale times the Coulomb constant) as
+    // a double-float pair: (h + l) * scale rounded once, in FP32
     constexpr double kScale = kMixScale * kElectroK;
+    constexpr float kScaleH = (float)kScale;
+    constexpr float kScaleL = (float)(kScale - (double)kScaleH);
+    // l2 is in q/r^2 units, the sums in the terms' scaled units
+    const float lim2 = (float)(P.kappa2 * (kMixScale * kMixScale));
     float ex[KL], ey[KL], ez[KL];
     bool redo[KL];
 #pragma unroll
@@ -283,13 +317,11 @@ __device__ __forceinline__ void finish_mixed(const RefTraceParams<float> &P, int
         group_two_sum<TPL>(hy[k]);
         group_two_sum<TPL>(hz[k]);
         const float l2s = group_sum<float, TPL>(l2[k]);
-        const double sx = (double)hx[k].h + (double)hx[k].l;
-        const double sy = (double)hy[k].h + (double)hy[k].l;
-        const double sz = (double)hz[k].h + (double)hz[k].l;
-        redo[k] = own[k] && (double)l2s > P.kappa2 * (sx * sx + sy * sy + sz * sz);
-        ex[k] = (float)(sx * kScale);
-        ey[k] = (float)(sy * kScale);
-        ez[k] = (float)(sz * kScale);
+        const float h2 = fmaf(hx[k].h, hx[k].h, fmaf(hy[k].h, hy[k].h, hz[k].h * hz[k].h));
+        redo[k] = own[k] && l2s > lim2 * h2;
+        ex[k] = fmaf(hx[k].h, kScaleH, fmaf(hx[k].h, kScaleL, hx[k].l * kScaleH));
+        ey[k] = fmaf(hy[k].h, kScaleH, fmaf(hy[k].h, kScaleL, hy[k].l * kScaleH));
+        ez[k] = fmaf(hz[k].h, kScaleH, fmaf(hz[k].h, kScaleL, hz[k].l * kScaleH));
     }
 #pragma unroll
     for (int k = 0; k < KL; ++k) {
@@ -301,8 +333,7 @@ __device__ __forceinline__ void finish_mixed(const RefTraceParams<float> &P, int
             const float ry = __shfl_sync(0xffffffffu, py[k], src);
             const float rz = __shfl_sync(0xffffffffu, pz[k], src);
             double fx, fy, fz;
-            refine_df_warp(static_cast<const float4 *>(P.charges), P.p_pad, P.tile_recs, lane,
-                           rx, ry, rz, fx, fy, fz);
+            refine_df_warp(rec, P.p_pad, P.tile_recs, lane, rx, ry, rz, fx, fy, fz);
             if (lane / TPL == src / TPL) {
                 ex[k] = (float)(fx * kElectroK);
                 ey[k] = (float)(fy * kElectroK);
@@ -329,12 +360,19 @@ __device__ __forceinline__ void finish_mixed(const RefTraceParams<float> &P, int
         }
         float sx, sy, sz;
         step_of<float>(ex[k], ey[k], ez[k], r0x, r0y, r0z, curvature, P.resolution, sx, sy, sz);
-        qx[k] += (double)sx;
-        qy[k] += (double)sy;
-        qz[k] += (double)sz;
-        px[k] = (float)qx[k];
-        py[k] = (float)qy[k];
-        pz[k] = (float)qz[k];
+        // the FP64 position on the group's first lane, its FP32 copy to all
+        if (t == 0) {
+            qx[k] += (double)sx;
+            qy[k] += (double)sy;
+            qz[k] += (double)sz;
+            px[k] = (float)qx[k];
+            py[k] = (float)qy[k];
+            pz[k] = (float)qz[k];
+        }
+        const int lead = lane & ~(TPL - 1);
+        px[k] = __shfl_sync(0xffffffffu, px[k], lead);
+        py[k] = __shfl_sync(0xffffffffu, py[k], lead);
+        pz[k] = __shfl_sync(0xffffffffu, pz[k], lead);
         if (own[k] && t == 0) {
             const size_t idx = (size_t)step * n + (size_t)line[k];
             store_stream(P.x + idx, px[k]);
@@ -500,7 +538,12 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                     continue;
             }
             if constexpr (ARITH == ARITH_MIXED) {
-                finish_mixed<TPL, KL>(P, step, t, lane, line, own, px, py, pz, qx, qy, qz, hx,
+                // re-evaluations read the records from shared memory when
+                // they are resident there, else from the staged copy
+                finish_mixed<TPL, KL>(P,
+                                      streamed ? static_cast<const float4 *>(P.charges)
+                                               : reinterpret_cast<const float4 *>(tiles),
+                                      step, t, lane, line, own, px, py, pz, qx, qy, qz, hx,
                                       hy, hz, l2);
                 continue;
             }
