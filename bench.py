@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--kl", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--pack", default="auto")
+    ap.add_argument("--mode", choices=["replicas", "shard"], default="replicas",
+                    help="N > 1: every rank traces the whole workload (weak "
+                         "scaling) or its contiguous shard of the lines "
+                         "(strong scaling, no exchange while tracing)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
@@ -142,7 +146,8 @@ def workload_config(args, n, p, rows, world, arith):
             "rows": int(rows), "seed": args.seed,
             "rule": "curvature, seed vector (CPU_Implement.cpp:207-351)",
             "arith": arith,
-            "parallelism": f"replicas x{world}",
+            "parallelism": (f"lines sharded x{world}" if getattr(args, "mode", "") == "shard"
+                            else f"replicas x{world}"),
             "l2": "vertex output %.2f GB per step exceeds the 129 MB L2"
                   % (3 * 4 * n * rows / 1e9)}
 
@@ -204,7 +209,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sample["seconds"] * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "strong" if getattr(args, "mode", "") == "shard" else "weak",
+        "vs_baseline": None, "dtype": "f32",
         "data": DATA,
         "config": workload_config(
             args, len(seeds), len(ch), rows, args.gpus,
@@ -322,8 +328,15 @@ def main():
     em = importlib.import_module("electromag-with-cuda_gb300")
     lib = em.load()
     ch, seeds, rows = workload(em, args.workload, args.seed + 0, args.rows)
-    n, p = len(seeds), len(ch)
-    pairs = float(n) * (rows - 1) * p
+    n_all, p = len(seeds), len(ch)
+    # strong scaling: this rank's contiguous shard of the lines
+    shard = args.mode == "shard" and world > 1
+    if shard:
+        b, e = em.shard.shard_range(n_all, world, rank)
+        seeds = seeds[b:e]
+    n = len(seeds)
+    pairs = float(n) * (rows - 1) * p           # this rank's work per step
+    pairs_all = float(n_all) * (rows - 1) * p * (1 if shard else world)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     X = [torch.zeros(n * rows, dtype=torch.float32, device=dev) for _ in range(3)]
@@ -367,13 +380,13 @@ def main():
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = pairs * world * args.steps / (ms * 1e-3) / 1e9
+    value = pairs_all * args.steps / (ms * 1e-3) / 1e9
     kernel_s = float(np.mean(kern))
     achieved = FLOP_PER_PAIR * pairs / kernel_s / 1e12
 
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(em, torch, dist, ch, seeds, rows, args, world)
+        e2e = run_e2e(em, torch, dist, ch, seeds, rows, args, pairs_all)
 
     extras = {}
     field_err = None
@@ -401,9 +414,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "strong" if shard else "weak", "vs_baseline": None, "dtype": "f32",
         "data": DATA,
-        "config": workload_config(args, n, p, rows, world,
+        "config": workload_config(args, n_all, p, rows, world,
                                   "fast FP32 (rsqrt + FMA)"),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops,
                      "unit": "TFLOP/s", "frac": achieved / peak_tflops,
@@ -499,6 +512,9 @@ def metric_parts(value, extras, value_err=None):
         parts["adjoint_over_forward"] = adj["stored"]["adjoint_over_forward"]
         parts["adjoint_over_forward_checkpointed"] = (
             adj["checkpoint"]["adjoint_over_forward"])
+        parts["adjoint_grad_rel_err_vs_fp64"] = max(
+            adj[m].get("grad_rel_err_vs_fp64", float("nan"))
+            for m in ("stored", "checkpoint"))
     return parts
 
 
@@ -615,6 +631,30 @@ def adjoint_block(em, torch, dev, seed):
                      "loss": float(loss.item()),
                      "grad_norm": float(grad.norm().item())}
     blk["checkpoint_rows"] = 64
+    # correctness at this scale: on 256 of the lines (all 4000 rows, all
+    # 1024 charges) the gradient of both modes against the FP64 discrete
+    # adjoint linearised at the GPU's own trajectory (the oracle, on the host)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import em_oracle as orc
+    sub = torch.from_numpy(np.linspace(0, n - 1, 256).astype(np.int64)).to(dev)
+    Ws = W[:, :, sub].contiguous()
+    Ts = T[:, :, sub].contiguous()
+    ref = None
+    for mode, ck in (("stored", False), ("checkpoint", True)):
+        loss, grad, _, _ = em.adjoint_device(Ws, ch, Ts, checkpoint=ck)
+        torch.cuda.synchronize()
+        if ref is None:
+            t0 = time.perf_counter()
+            ref = orc.adjoint_at(ch_np.astype(np.float64), Ws.double().cpu().numpy(),
+                                 Ts.double().cpu().numpy())
+            blk["grad_check_host_s"] = time.perf_counter() - t0
+        L, g = ref
+        gg = grad.cpu().numpy()
+        blk[mode]["grad_rel_err_vs_fp64"] = float(np.linalg.norm(gg - g) /
+                                                  np.linalg.norm(g))
+        blk[mode]["loss_rel_err_vs_fp64"] = abs(float(loss.item()) - L) / abs(L)
+    blk["grad_check"] = ("256 of the lines, all rows and charges, against the "
+                         "FP64 discrete adjoint linearised at the GPU trajectory")
     return blk
 
 
@@ -958,9 +998,10 @@ def lib_peak(lib):
     return t.value
 
 
-def run_e2e(em, torch, dist, ch, seeds, rows, args, world):
+def run_e2e(em, torch, dist, ch, seeds, rows, args, pairs_all):
     """Host-pointer C ABI calls on pinned buffers: seeds and charges go in,
-    every vertex comes out, each step."""
+    every vertex comes out, each step; pairs_all is the pair count of one
+    step over all ranks."""
     n, p = len(seeds), len(ch)
     H = [torch.zeros(n * rows, dtype=torch.float32).pin_memory()
          for _ in range(3)]
@@ -991,7 +1032,7 @@ def run_e2e(em, torch, dist, ch, seeds, rows, args, world):
         tt = torch.tensor([sec], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         sec = float(tt.item())
-    pairs = float(n) * (rows - 1) * p * world * args.steps
+    pairs = pairs_all * args.steps
     return {"value": pairs / sec / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": 3 * 4 * n + 16 * p,
             "d2h_bytes_per_step": 3 * 4 * n * (rows - 1) + 4}

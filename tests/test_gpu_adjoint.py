@@ -141,3 +141,47 @@ def test_adjoint_fixed_step_mode(em, gpu, adjoint_case, orc):
     L = float(((V - targets.astype(np.float64)) ** 2).sum())
     assert out["loss"] == pytest.approx(L, rel=1e-4)
     assert np.all(np.isfinite(out["grad"]))
+
+
+@pytest.fixture(scope="module")
+def scale_case(em):
+    """The adjoint benchmark's charge set (1024 charges uniform in a cube of
+    side 100) and length (4000 rows: 62 checkpoint segments and a partial
+    one), 256 of its lines; targets a seeded perturbation of the forward."""
+    torch = pytest.importorskip("torch")
+    ch, seeds, rows = em.workloads.make("adjoint_1024", seed=1234)
+    idx = np.linspace(0, len(seeds) - 1, 256).astype(int)
+    n = len(idx)
+    V = torch.zeros((3, rows, n), dtype=torch.float32, device="cuda")
+    V[:, 0, :] = torch.from_numpy(seeds[idx].T.astype(np.float32)).cuda()
+    dch = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).cuda()
+    rc, _ = em.calc_field(V[0].reshape(-1), V[1].reshape(-1), V[2].reshape(-1),
+                          dch, n, 1.0, True, require_n64=False)
+    assert rc == 0
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    T = V + 0.1 * torch.randn(V.shape, generator=gen, device="cuda")
+    W = torch.zeros_like(V)
+    W[:, 0, :] = V[:, 0, :]
+    return ch, dch, W, T
+
+
+@pytest.mark.parametrize("checkpoint", [False, True])
+def test_adjoint_at_benchmark_scale(em, gpu, orc, scale_case, checkpoint):
+    """Gradients with respect to all 1024 x 3 positions and 1024 magnitudes
+    over 4000 rows: against the FP64 discrete adjoint linearised at the
+    GPU's own trajectory (the FP32 and FP64 trajectories part where lines
+    circle charges), within 1e-4 overall and on each of the 32 largest
+    entries."""
+    ch, dch, W, T = scale_case
+    loss, grad, _, _ = em.adjoint_device(W, dch, T, checkpoint=checkpoint)
+    import torch
+    torch.cuda.synchronize()
+    L, g = orc.adjoint_at(ch.astype(np.float64), W.double().cpu().numpy(),
+                          T.double().cpu().numpy())
+    gg = grad.cpu().numpy()
+    assert float(loss.item()) == pytest.approx(L, rel=1e-6)
+    assert rel(gg, g) <= GRAD_RTOL
+    big = np.argsort(-np.abs(g).ravel())[:32]
+    assert np.all(np.abs(gg.ravel()[big] - g.ravel()[big])
+                  <= GRAD_RTOL * np.abs(g.ravel()[big]))

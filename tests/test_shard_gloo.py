@@ -115,3 +115,63 @@ def test_sharded_adjoint_equals_single_process(em, orc, tmp_path):
         z = np.load(out + f".{r}.npz")
         assert float(z["loss"]) == pytest.approx(fz.L, rel=1e-12)
         assert np.allclose(z["grad"], ref_g, rtol=1e-10, atol=1e-12 * np.abs(ref_g).max())
+
+
+def _trace_worker(rank, world, port, out_path):
+    """bench.py's sharded mode on CPU ranks: shard the lines, trace each
+    shard (here with the oracle's restatement of the reference's FP32 path,
+    where bench.py calls the GPU tracer), gather along the line axis."""
+    import importlib
+    import sys
+    import torch.distributed as dist
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    sys.path.insert(0, os.path.join(root, "oracle"))
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    em = importlib.import_module("electromag-with-cuda_gb300")
+    import em_oracle as orc
+    ch, seeds, rows = _trace_inputs(em)
+
+    def trace(s):
+        X = [np.zeros(len(s) * rows, np.float32) for _ in range(3)]
+        for c in range(3):
+            X[c][:len(s)] = s[:, c]
+        # the generic curvature rule takes any line count (the SSE form
+        # wants multiples of 64)
+        assert orc.calc_field(*X, ch, len(s), 1.0, orc.CURV_GENERIC, nthreads=1) == 0
+        return np.stack([x.reshape(rows, len(s)) for x in X])
+
+    V, (b, e) = em.shard.trace_sharded(trace, seeds, world, rank)
+    np.savez(out_path + f".{rank}.npz", V=V, b=b, e=e)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def _trace_inputs(em):
+    ch, seeds, _ = em.workloads.make("cpu_256", seed=9)
+    # 1001 lines: the ranks' shards differ in size (500 and 501)
+    seeds = np.resize(seeds.astype(np.float32), (1001, 3))
+    return np.ascontiguousarray(ch, np.float32), seeds, 40
+
+
+def test_sharded_trace_gathers_the_single_process_result(em, orc, tmp_path):
+    """Two gloo ranks trace 500 and 501 lines of one workload; after the
+    gather both hold the vertices of the whole trace, bit for bit those of
+    one process tracing every line."""
+    out = str(tmp_path / "tr")
+    mp.spawn(_trace_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    ch, seeds, rows = _trace_inputs(em)
+    n = len(seeds)
+    X = [np.zeros(n * rows, np.float32) for _ in range(3)]
+    for c in range(3):
+        X[c][:n] = seeds[:, c]
+    assert orc.calc_field(*X, ch, n, 1.0, orc.CURV_GENERIC) == 0
+    ref = np.stack([x.reshape(rows, n) for x in X])
+    spans = []
+    for r in range(2):
+        z = np.load(out + f".{r}.npz")
+        assert np.array_equal(z["V"], ref)
+        spans.append((int(z["b"]), int(z["e"])))
+    assert spans == [(0, 501), (501, 1001)]
