@@ -632,29 +632,49 @@ def adjoint_block(em, torch, dev, seed):
                      "grad_norm": float(grad.norm().item())}
     blk["checkpoint_rows"] = 64
     # correctness at this scale: on 256 of the lines (all 4000 rows, all
-    # 1024 charges) the gradient of both modes against the FP64 discrete
-    # adjoint linearised at the GPU's own trajectory (the oracle, on the host)
+    # 1024 charges) the gradient of both modes against the FP64 adjoint of
+    # the GPU's own frozen map (linearised at its trajectory with the field
+    # its forward used, traced again here with the field output in the
+    # adjoint's shape), and against the FP64 adjoint with the FP64 field at
+    # the same vertices (the sensitivity to the forward field's rounding)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import em_oracle as orc
     sub = torch.from_numpy(np.linspace(0, n - 1, 256).astype(np.int64)).to(dev)
-    Ws = W[:, :, sub].contiguous()
+    ns = 256
+    Vs = torch.zeros((3, rows, ns), dtype=torch.float32, device=dev)
+    Vs[:, 0, :] = V[:, 0, sub]
+    Fs = torch.zeros(3 * ns * (rows - 1), dtype=torch.float32, device=dev)
+    rc, _ = em.calc_field(Vs[0].reshape(-1), Vs[1].reshape(-1), Vs[2].reshape(-1),
+                          ch, ns, 1.0, True, require_n64=False, field_out=Fs,
+                          threads_per_line=8, lines_per_thread=1)
+    if rc:
+        raise em.EmError(rc, "forward with field output")
     Ts = T[:, :, sub].contiguous()
-    ref = None
+    Ws = torch.zeros_like(Vs)
+    Ws[:, 0, :] = Vs[:, 0, :]
+    refs = None
     for mode, ck in (("stored", False), ("checkpoint", True)):
         loss, grad, _, _ = em.adjoint_device(Ws, ch, Ts, checkpoint=ck)
         torch.cuda.synchronize()
-        if ref is None:
+        if refs is None:
             t0 = time.perf_counter()
-            ref = orc.adjoint_at(ch_np.astype(np.float64), Ws.double().cpu().numpy(),
-                                 Ts.double().cpu().numpy())
+            chd = ch_np.astype(np.float64)
+            Wh, Th = Ws.double().cpu().numpy(), Ts.double().cpu().numpy()
+            refs = (orc.adjoint_at_field(chd, Wh, Th, Fs.view(3, rows - 1, ns)
+                                         .double().cpu().numpy()),
+                    orc.adjoint_at(chd, Wh, Th))
             blk["grad_check_host_s"] = time.perf_counter() - t0
-        L, g = ref
+        (L, g), (_, g64) = refs
         gg = grad.cpu().numpy()
         blk[mode]["grad_rel_err_vs_fp64"] = float(np.linalg.norm(gg - g) /
                                                   np.linalg.norm(g))
+        blk[mode]["grad_rel_diff_vs_fp64_field"] = float(
+            np.linalg.norm(gg - g64) / np.linalg.norm(g64))
         blk[mode]["loss_rel_err_vs_fp64"] = abs(float(loss.item()) - L) / abs(L)
-    blk["grad_check"] = ("256 of the lines, all rows and charges, against the "
-                         "FP64 discrete adjoint linearised at the GPU trajectory")
+    blk["grad_check"] = ("256 of the lines, all rows and charges: against the "
+                         "FP64 discrete adjoint of the GPU's frozen map (its "
+                         "trajectory and forward field); the second figure "
+                         "with the FP64 field at the same vertices instead")
     return blk
 
 

@@ -389,6 +389,27 @@ static double frozen_lambda(const double *ep, const double *p0, double res)
     return 1.0 / ((kc + 1.0) * res);
 }
 
+/* lam as the FP32 trace steps: the reference's single-precision sequence
+ * (CPU_Implement.cpp:322-331) from E = K E' rounded to FP32 (the field an
+ * FP32 forward stepped with), curvature against the FP32 seed; each
+ * operation rounded once (the oracle is built without contraction). */
+static double frozen_lambda_f32(const double *ep, const double *p0, double res)
+{
+    const double K = ORC_ELECTRO_K;
+    const float ex = (float)(K * ep[0]), ey = (float)(K * ep[1]), ez = (float)(K * ep[2]);
+    const float px = (float)p0[0], py = (float)p0[1], pz = (float)p0[2];
+    float k2 = ex * ex;
+    k2 = k2 + ey * ey;
+    k2 = k2 + ez * ez;
+    const float ix = ex - px, iy = ey - py, iz = ez - pz;
+    const float cx = iy * pz - iz * py, cy = iz * px - ix * pz, cz = ix * py - iy * px;
+    float c2 = cx * cx;
+    c2 = c2 + cy * cy;
+    c2 = c2 + cz * cz;
+    const float kc = sqrtf(c2) / (k2 * sqrtf(k2));
+    return (double)(1.0f / ((kc + 1.0f) * (float)res));
+}
+
 double orc_frozen_loss_f64(const double *charges, size_t p, const double *sx,
                            const double *sy, const double *sz, size_t n,
                            size_t S, double res, const double *tx,
@@ -473,7 +494,7 @@ static void adjoint_sweep(const double *charges, size_t p, const double *vx,
                           const double *vy, const double *vz, size_t n, size_t S,
                           double res, int curvature, const double *tx,
                           const double *ty, const double *tz, const double *lam_in,
-                          double *grad)
+                          const double *const *fe, int lam_fp32, double *grad)
 {
     for (size_t l = 0; l < n; ++l) {
         const size_t last = (S - 1) * n + l;
@@ -484,9 +505,17 @@ static void adjoint_sweep(const double *charges, size_t p, const double *vx,
             const size_t i = s * n + l;
             const double v[3] = {vx[i], vy[i], vz[i]};
             double e[3];
-            field_prime(charges, p, v[0], v[1], v[2], e);
-            const double lam = lam_in ? lam_in[i]
-                               : curvature ? frozen_lambda(e, p0, res) : 1.0 / res;
+            if (fe) {
+                e[0] = fe[0][i];
+                e[1] = fe[1][i];
+                e[2] = fe[2][i];
+            } else {
+                field_prime(charges, p, v[0], v[1], v[2], e);
+            }
+            const double lam = lam_in     ? lam_in[i]
+                               : !curvature ? 1.0 / res
+                               : lam_fp32   ? frozen_lambda_f32(e, p0, res)
+                                            : frozen_lambda(e, p0, res);
             const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
             const double u[3] = {e[0] / en, e[1] / en, e[2] / en};
             const double ua = u[0] * a[0] + u[1] * a[1] + u[2] * a[2];
@@ -526,7 +555,7 @@ double orc_frozen_grad_f64(const double *charges, size_t p, const double *sx,
                                          tz, lam_in, NULL, vx, vy, vz);
     for (size_t k = 0; k < 4 * p; ++k)
         grad[k] = 0;
-    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, 1, tx, ty, tz, lam_in, grad);
+    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, 1, tx, ty, tz, lam_in, NULL, 0, grad);
     free(vx);
     free(vy);
     free(vz);
@@ -545,6 +574,27 @@ double orc_adjoint_at_f64(const double *charges, size_t p, const double *vx,
     }
     for (size_t k = 0; k < 4 * p; ++k)
         grad[k] = 0;
-    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, curvature, tx, ty, tz, NULL, grad);
+    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, curvature, tx, ty, tz, NULL, NULL, 0,
+                  grad);
+    return L;
+}
+
+double orc_adjoint_at_field_f64(const double *charges, size_t p, const double *vx,
+                                const double *vy, const double *vz, size_t n, size_t S,
+                                double res, int curvature, const double *tx,
+                                const double *ty, const double *tz, const double *fx,
+                                const double *fy, const double *fz, int lam_fp32,
+                                double *grad)
+{
+    double L = 0;
+    for (size_t i = 0; i < S * n; ++i) {
+        const double dx = vx[i] - tx[i], dy = vy[i] - ty[i], dz = vz[i] - tz[i];
+        L += dx * dx + dy * dy + dz * dz;
+    }
+    for (size_t k = 0; k < 4 * p; ++k)
+        grad[k] = 0;
+    const double *fe[3] = {fx, fy, fz};
+    adjoint_sweep(charges, p, vx, vy, vz, n, S, res, curvature, tx, ty, tz, NULL, fe, lam_fp32,
+                  grad);
     return L;
 }

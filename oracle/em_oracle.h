@@ -145,6 +145,18 @@ double orc_adjoint_at_f64(const double *charges, size_t p, const double *vx,
                           const double *vy, const double *vz, size_t n, size_t S,
                           double res, int curvature, const double *tx,
                           const double *ty, const double *tz, double *grad);
+/* The same with the field E' = E/K at each vertex given (fx, fy, fz: the
+ * S-1 rows the steps used, e.g. a GPU forward's own field) instead of
+ * recomputed in FP64: the step lengths, directions and |E'| of the frozen
+ * map are those of the given field, the Jacobian products stay FP64 sums.
+ * lam_fp32: the step lengths by the reference's FP32 step sequence from the
+ * field rounded to FP32 (exactly those an FP32 forward took); 0: in FP64. */
+double orc_adjoint_at_field_f64(const double *charges, size_t p, const double *vx,
+                                const double *vy, const double *vz, size_t n, size_t S,
+                                double res, int curvature, const double *tx,
+                                const double *ty, const double *tz, const double *fx,
+                                const double *fy, const double *fz, int lam_fp32,
+                                double *grad);
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
 CURV_SSE, CURV_GENERIC, FIXED = 0, 1, 2
+# electro_k of include/Electrostatics.h:27 (the oracle's ORC_ELECTRO_K)
+ELECTRO_K = 8.987551787e9
 TERM_STEPS, TERM_CHARGE, TERM_NULL = 0, 1, 2
 
 P, S, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
@@ -55,6 +57,9 @@ def load():
         lib.orc_adjoint_at_f64.restype = D
         lib.orc_adjoint_at_f64.argtypes = [P, S, P, P, P, S, S, D, I, P, P,
                                            P, P]
+        lib.orc_adjoint_at_field_f64.restype = D
+        lib.orc_adjoint_at_field_f64.argtypes = [P, S, P, P, P, S, S, D, I, P,
+                                                 P, P, P, P, P, I, P]
         _lib = lib
     return _lib
 
@@ -137,6 +142,31 @@ def adjoint_at(charges, V, targets, resolution=1.0, curvature=True):
     g = np.zeros(ch.size)
     L = lib.orc_adjoint_at_f64(_p(ch), len(ch), *map(_p, V), n, S, resolution,
                                int(bool(curvature)), *map(_p, T), _p(g))
+    return L, g.reshape(-1, 4)
+
+
+def adjoint_at_field(charges, V, targets, F, resolution=1.0, curvature=True,
+                     lam_fp32=True):
+    """adjoint_at with the field each step used given: F (3, S-1, n) with
+    the Coulomb constant applied (a forward's own field output); the frozen
+    map's directions and |E| come from it and, with lam_fp32, its step
+    lengths by the reference's FP32 step sequence (those the FP32 forward
+    took; else in FP64); the Jacobian products are FP64 sums.  Returns
+    (L, grad (p, 4))."""
+    lib = load()
+    ch = np.ascontiguousarray(charges, np.float64)
+    V = [np.ascontiguousarray(np.asarray(V[c], np.float64).reshape(-1))
+         for c in range(3)]
+    T = [np.ascontiguousarray(np.asarray(targets[c], np.float64).reshape(-1))
+         for c in range(3)]
+    S, n = np.asarray(targets[0]).shape
+    Fe = [np.ascontiguousarray(np.asarray(F[c], np.float64).reshape(-1) / ELECTRO_K)
+          for c in range(3)]
+    g = np.zeros(ch.size)
+    L = lib.orc_adjoint_at_field_f64(_p(ch), len(ch), *map(_p, V), n, S,
+                                     resolution, int(bool(curvature)),
+                                     *map(_p, T), *map(_p, Fe),
+                                     int(bool(lam_fp32)), _p(g))
     return L, g.reshape(-1, 4)
 
 

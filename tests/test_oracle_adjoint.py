@@ -72,3 +72,17 @@ def test_adjoint_at_benchmark_length(adjoint_scale_case):
     for j, c in sampled:
         fd = fz.central(j, c, 1e-3)
         assert abs(g[j, c] - fd) <= 1e-3 * abs(fd) + 1e-6 * np.abs(g).max()
+
+
+def test_adjoint_at_given_fp64_field_equals_adjoint_at(orc, adjoint_case):
+    """Given the FP64 field at each vertex, the at-field adjoint is the
+    at-trajectory adjoint (the field is what the latter recomputes)."""
+    ch, seeds, rows, targets, fz = adjoint_case
+    V = np.stack([v.reshape(rows, -1) for v in fz.V])
+    n = V.shape[2]
+    pts = V[:, :-1, :].reshape(3, -1).T
+    F = orc.field_f64(pts, ch).T.reshape(3, rows - 1, n)
+    L1, g1 = orc.adjoint_at(ch, V, targets)
+    L2, g2 = orc.adjoint_at_field(ch, V, targets, F, lam_fp32=False)
+    assert L1 == L2
+    assert np.allclose(g2, g1, rtol=0, atol=1e-12 * np.abs(g1).max())
