@@ -236,10 +236,19 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     if (pl.arith == ARITH_MIXED)
         prm.group_ctr = reinterpret_cast<unsigned long long *>(
             static_cast<unsigned char *>(c.errbuf) + 40);
-    if (o.field_out) {
-        prm.ox = static_cast<T *>(o.field_out);
-        prm.oy = prm.ox + n * (total_steps - 1);
-        prm.oz = prm.oy + n * (total_steps - 1);
+    // field output: the mixed form stores its final field itself; the fast
+    // and exact forms use their stored-field slot (the sum before the fast
+    // form's Coulomb factor, which a small kernel applies afterwards)
+    T *fout = static_cast<T *>(o.field_out);
+    const size_t fcount = n * (total_steps - 1);
+    if (fout && pl.arith == ARITH_MIXED) {
+        prm.ox = fout;
+        prm.oy = fout + fcount;
+        prm.oz = fout + 2 * fcount;
+    } else if (fout) {
+        prm.fx = fout;
+        prm.fy = fout + fcount;
+        prm.fz = fout + 2 * fcount;
     }
 
     // Host arrays, all lines: trace in row chunks and copy each finished
@@ -304,6 +313,8 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
         if (e == cudaSuccess)
             e = cudaStreamWaitEvent(s, c.ev_chunk, 0);
     }
+    if (e == cudaSuccess && fout && pl.arith != ARITH_MIXED && pl.arith != ARITH_EXACT)
+        e = launch_scale_coulomb<T>(fout, 3 * fcount, s);
     if (e != cudaSuccess)
         return map_cuda(e);
     if (chunked) {

@@ -66,8 +66,8 @@ template <class T> struct RefTraceParams {
     // test, and the count of re-evaluated vertices (null: not counted)
     double kappa2;
     unsigned long long *refines;
-    // optional: the field each step uses (Coulomb constant applied, after
-    // any re-evaluation), stored like fx (null: none)
+    // optional, mixed arithmetic: the field each step uses (Coulomb constant
+    // applied, after any re-evaluation), stored like fx (null: none)
     T *ox, *oy, *oz;
     // optional (resident charges only): a zeroed counter from which warps
     // take line groups in order instead of the fixed round-robin deal
@@ -260,6 +260,8 @@ constexpr int kUnroll = 8;
 template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,
                              cudaStream_t stream);
+// v[0, m) *= the Coulomb constant, rounded as the tracer rounds it.
+template <class T> cudaError_t launch_scale_coulomb(T *v, size_t m, cudaStream_t stream);
 
 // Stages p raw charge records into p_pad records (pad record {1e15, 1e15,
 // 1e15, 0}, whose contribution is exactly zero), plain (paired = 0) or in

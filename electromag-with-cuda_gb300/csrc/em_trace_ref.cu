@@ -19,6 +19,8 @@
 // no contraction), which reproduces the strict x86 build bit for bit.  The
 // per-vertex step (curvature, vec3SetInvLen, include/Vector.h:157-164) uses
 // the IEEE sequence in both modes.
+#include <algorithm>
+
 #include "em_device.cuh"
 #include "em_ext.cuh"
 #include "em_internal.h"
@@ -469,7 +471,8 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
     // Groups: dealt round-robin to CTAs, or, with resident charges and a
     // group counter (the mixed form, whose re-evaluations make some groups
     // slower than others), taken one at a time by whichever warp is free.
-    const bool queued = !streamed && P.group_ctr;
+    constexpr bool kQueue = ARITH == ARITH_MIXED;
+    const bool queued = kQueue && !streamed && P.group_ctr;
     uint32_t it = 0;
     for (int r = 0; queued || r < rounds; ++r) {
         long long gk = (long long)r * ncw + warp;
@@ -577,12 +580,6 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                     r0x = ld_seed(P.seed_x + line[k]);
                     r0y = ld_seed(P.seed_y + line[k]);
                     r0z = ld_seed(P.seed_z + line[k]);
-                }
-                if (P.ox && own[k] && t == 0) {
-                    const size_t fi = (size_t)(step - 1) * n + (size_t)line[k];
-                    store_stream(P.ox + fi, ax);
-                    store_stream(P.oy + fi, ay);
-                    store_stream(P.oz + fi, az);
                 }
                 advance<T>(ax, ay, az, r0x, r0y, r0z, curvature, P.resolution, px[k], py[k],
                            pz[k]);
@@ -728,6 +725,33 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &params, const LaunchCfg &c
     default: return cudaErrorInvalidValue;
     }
 }
+
+namespace {
+
+// v *= K with the kernel's own rounding (mul_rn), over m values: the field
+// the fast arithmetic stored before its per-vertex Coulomb factor.
+template <class T> __global__ void scale_k_kernel(T *v, size_t m)
+{
+    const T K = (T)kElectroK;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (size_t)gridDim.x * blockDim.x)
+        v[i] = mul_rn(v[i], K);
+}
+
+} // namespace
+
+template <class T> cudaError_t launch_scale_coulomb(T *v, size_t m, cudaStream_t stream)
+{
+    if (!m)
+        return cudaSuccess;
+    const size_t blocks = std::min<size_t>((m + 255) / 256, 152 * 16);
+    scale_k_kernel<T><<<(unsigned)blocks, 256, 0, stream>>>(v, m);
+    count_launch(1);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_scale_coulomb<float>(float *, size_t, cudaStream_t);
+template cudaError_t launch_scale_coulomb<double>(double *, size_t, cudaStream_t);
 
 template <class T>
 cudaError_t launch_stage_charges(const void *raw, int p, void *staged, int p_pad, int paired,
