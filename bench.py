@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
-    ap.add_argument("--case", choices=["ext-fp32", "ext-mixed", "ext-df64",
+    ap.add_argument("--case", choices=["ref-mixed", "ext-fp32", "ext-mixed", "ext-df64",
                                        "ext-tail-dipole", "adjoint",
                                        "adjoint-checkpoint", "adjoint-twopass",
                                        "batch", "verlet"],
@@ -228,7 +228,8 @@ def run_reference(args):
 
 
 def run_case(args):
-    """Small profiling cases (ncu captures): the extended kernel on the
+    """Small profiling cases (ncu captures): the mixed arithmetic on the
+    reference-layout tracer (4096 charges, 200 rows), the extended kernel on the
     4096-charge workload (200 rows, no termination radius; FP32, mixed or
     double-float pairs), the extended tracer with its tail kernel on the
     dipole set (1000 rows, termination radius 0.5), the adjoint
@@ -241,6 +242,26 @@ def run_case(args):
     import torch
     em = importlib.import_module("electromag-with-cuda_gb300")
     dev = torch.device("cuda", 0)
+    if args.case == "ref-mixed":
+        # the mixed arithmetic on the reference-layout tracer, 4096-charge
+        # workload (--rows, default 200): once with the default conditioning
+        # test, once with re-evaluations off (the pair pass alone)
+        ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)
+        rows = args.rows or 200
+        n = len(seeds)
+        dch = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).to(dev)
+        for kappa in (0.0, 1e30):
+            X = [torch.zeros(n * rows, dtype=torch.float32, device=dev) for _ in range(3)]
+            for c in range(3):
+                X[c][:n] = torch.from_numpy(np.ascontiguousarray(seeds[:, c], np.float32)).to(dev)
+            rc, perf = em.calc_field(*X, dch, n, 1.0, True, arith="mixed",
+                                     require_n64=False, refine_kappa=kappa)
+            if rc:
+                raise em.EmError(rc, "mixed")
+            torch.cuda.synchronize()
+            print("mixed kappa", kappa or "default", n * (rows - 1) * len(ch) / perf.time / 1e9,
+                  "Gpair/s, re-evaluated vertices", perf.fp64_refines)
+        return 0
     if args.case == "batch":
         sets = em.workloads.make_batch(512, args.seed)[:24]
         lims = np.concatenate([np.full(len(s), min(lim, 500), np.int32)
