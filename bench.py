@@ -518,7 +518,7 @@ def metric_parts(value, extras, value_err=None):
             if "gpair_s" in mref:
                 cands.append(("reference-layout mixed", mref["gpair_s"],
                               mref["field_err"]["vs_fp64"]["max"]))
-        for mode in ("fp32", "mixed", "mixed_nf0.05", "mixed_nf0.05_df64", "df64", "fp64"):
+        for mode in ("fp32", "mixed", "mixed_fp64_refine", "mixed_no_refine", "df64", "fp64"):
             m = blk.get(mode) or {}
             err = (m.get("field_err_vs_fp64") or {}).get("max")
             if m.get("gpair_s"):
@@ -563,15 +563,15 @@ def field_errors(em, torch, ch, V, F, ln, samples, seed):
 
 
 def traced(em, torch, ch, seeds, steps, term, precision, want_field,
-           null_frac=0.0, refine="fp64"):
+           refine_kappa=0.0, refine="df64"):
     dt = torch.float64 if precision == "fp64" else torch.float32
     em.trace_lines(seeds.to(dt), ch.to(dt), min(steps, 8), 1.0, term,
-                   precision=precision, null_frac=null_frac,
+                   precision=precision, refine_kappa=refine_kappa,
                    refine=refine)  # warm-up
     torch.cuda.synchronize()
     out = em.trace_lines(seeds.to(dt), ch.to(dt), steps, 1.0, term,
                          precision=precision, want_field=want_field,
-                         null_frac=null_frac, refine=refine)
+                         refine_kappa=refine_kappa, refine=refine)
     torch.cuda.synchronize()
     perf = out["perf"]
     out["gpairs"] = perf.pairs / perf.time / 1e9 if perf.time > 0 else 0.0
@@ -580,20 +580,21 @@ def traced(em, torch, ch, seeds, steps, term, precision, want_field,
 
 def precision_block(em, torch, dev, name, steps, seed, samples, with_ratio):
     """FP32 / mixed / double-float / FP64 runs of the extended method on one
-    workload, with throughput and field error vs FP64; the mixed mode also
-    with null_frac 0.05, its re-evaluations in FP64 or in double-float."""
+    workload, with throughput and field error vs FP64; the mixed mode with
+    its default conditioning test and double-float re-evaluations, with FP64
+    re-evaluations, and with the re-evaluations off."""
     ch_np, seeds_np, _ = em.workloads.make(name, seed=seed)
     ch = torch.from_numpy(np.ascontiguousarray(ch_np, np.float32)).to(dev)
     seeds = torch.from_numpy(seeds_np.astype(np.float32)).to(dev)
     blk = {"workload": name, "lines": int(len(seeds_np)),
            "charges": int(len(ch_np)), "max_rows": steps,
            "term_radius": 0.5}
-    for prec, nf, refine in (("fp32", 0.0, "fp64"), ("mixed", 0.0, "fp64"),
-                             ("mixed_nf0.05", 0.05, "fp64"),
-                             ("mixed_nf0.05_df64", 0.05, "df64"),
-                             ("df64", 0.0, "fp64"), ("fp64", 0.0, "fp64")):
+    for prec, kappa, refine in (("fp32", 0.0, "df64"), ("mixed", 0.0, "df64"),
+                                ("mixed_fp64_refine", 0.0, "fp64"),
+                                ("mixed_no_refine", 1e30, "df64"),
+                                ("df64", 0.0, "df64"), ("fp64", 0.0, "df64")):
         p = "mixed" if prec.startswith("mixed") else prec
-        out = traced(em, torch, ch, seeds, steps, 0.5, p, True, nf, refine)
+        out = traced(em, torch, ch, seeds, steps, 0.5, p, True, kappa, refine)
         ln = out["len"]
         cls = np.bincount(out["cls"].cpu().numpy(), minlength=3)
         errs = field_errors(em, torch, ch, out["vertices"], out["field"], ln,

@@ -39,8 +39,8 @@ EM_PACK_PAIRS = 2
 EM_PREC_FP32 = 0
 EM_PREC_MIXED = 1
 EM_PREC_DF64 = 2
-EM_REFINE_FP64 = 0
-EM_REFINE_DF64 = 1
+EM_REFINE_DF64 = 0
+EM_REFINE_FP64 = 1
 EM_TERM_STEPS = 0
 EM_TERM_CHARGE = 1
 EM_TERM_NULL = 2

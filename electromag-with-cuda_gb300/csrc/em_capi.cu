@@ -229,7 +229,7 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     prm.rule = use_curvature ? o.rule : RULE_FIXED;
     prm.resolution = resolution;
     prm.err = c.err;
-    const double kappa = o.refine_kappa > 0 ? o.refine_kappa : kMixKappaDefault;
+    const double kappa = mix_kappa(o);
     prm.kappa2 = kappa * kappa;
     prm.refines = refines;
     // the mixed form's groups come from a queue (status word at byte 40)

@@ -49,7 +49,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
         return EM_ERR_ARG;
     if (o.refine != EM_REFINE_FP64 && o.refine != EM_REFINE_DF64)
         return EM_ERR_ARG;
-    if (!(term_radius >= 0) || !(o.null_frac >= 0))
+    if (!(term_radius >= 0) || !(o.null_frac >= 0) || !(o.refine_kappa >= 0))
         return EM_ERR_ARG;
     if (max_steps > (size_t)INT_MAX || p > (size_t)(INT_MAX / 64) ||
         n > (size_t)(LLONG_MAX / 64) / max_steps)
@@ -236,7 +236,11 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     prm.steps_per_line = dspl;
     prm.resolution = (double)resolution;
     prm.term_r2 = (double)term_radius * (double)term_radius;
-    prm.null_frac = o.null_frac > 0 ? o.null_frac : 1e-4;
+    prm.null_frac = o.null_frac;
+    {
+        const double kappa = mix_kappa(o);
+        prm.kappa2 = kappa * kappa;
+    }
     prm.len = dlen;
     prm.cls = dcls;
     prm.next_line = reinterpret_cast<unsigned long long *>(status + kOffNext);
@@ -248,7 +252,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     prm.stages = cfg.stages;
     prm.resident = cfg.resident;
     prm.regroup = o.deterministic ? 0 : 1;
-    prm.refine_df64 = o.refine == EM_REFINE_DF64 ? 1 : 0;
+    prm.refine_fp64 = o.refine == EM_REFINE_FP64 ? 1 : 0;
     prm.err = c.err;
     prm.cont = c.tail;
     prm.cont_count = reinterpret_cast<unsigned long long *>(status + kOffContCount);

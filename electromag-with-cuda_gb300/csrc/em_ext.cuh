@@ -91,12 +91,13 @@ __device__ __forceinline__ void pairs_fast(const ChargeD *tile, int jneg, int co
 }
 
 // Mixed: FP32 pairs with the inv^3 correction over records [lo, hi) (lo a
-// multiple of TPL), compensated every kChunk pairs; dmin gets the nearest
-// distance^2 of the range.
-template <int TPL>
+// multiple of TPL), compensated every kChunk pairs; l2 gets the sum of the
+// terms' squared sizes q^2/r^4 (the conditioning test's measure) and, for
+// NEG (the negative block), dmin the nearest distance^2 of the range.
+template <int TPL, bool NEG>
 __device__ __forceinline__ void mixed_range(const float4 *tile, int lo, int hi, int t, float px,
                                             float py, float pz, CF &hx, CF &hy, CF &hz,
-                                            float &dmin)
+                                            float &dmin, float &l2)
 {
     for (int j0 = lo + t; j0 < hi; j0 += TPL * kChunk) {
         const int j1 = min(hi, j0 + TPL * kChunk);
@@ -106,15 +107,18 @@ __device__ __forceinline__ void mixed_range(const float4 *tile, int lo, int hi, 
             const float4 c = tile[j];
             const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            dmin = fminf(dmin, r2);
+            if (NEG)
+                dmin = fminf(dmin, r2);
             const float inv = rsqrt_fast(r2);
             const float inv2 = inv * inv;
-            const float s0 = (c.w * inv) * inv2;
+            const float qi = c.w * inv;
+            const float s0 = qi * inv2;
             // inv^3 carries three times the relative error eps of inv; to
             // first order r2 inv2 - 1 = 2 eps, so s0 (2.5 - 1.5 r2 inv2) =
             // s0 / (1 + 3 eps): one Newton correction, three FMA-pipe ops
             const float g = fmaf(-1.5f * r2, inv2, 2.5f);
             const float sc = s0 * g;
+            l2 = fmaf(qi, s0, l2);
             ax = fmaf(sc, dx, ax);
             ay = fmaf(sc, dy, ay);
             az = fmaf(sc, dz, az);
@@ -125,16 +129,17 @@ __device__ __forceinline__ void mixed_range(const float4 *tile, int lo, int hi, 
     }
 }
 
+// Mixed pairs over a tile: [0, jneg) are negative charges (nearest one
+// tracked); l2 sums q^2/r^4 over every pair.
 template <int TPL>
 __device__ __forceinline__ void pairs_mixed(const float4 *tile, int jneg, int count, int t,
                                             float px, float py, float pz, CF &hx, CF &hy, CF &hz,
-                                            float &dneg, float &dall)
+                                            float &dneg, float &l2)
 {
-    float dn = 3.0e38f, dp = 3.0e38f;
-    mixed_range<TPL>(tile, 0, jneg, t, px, py, pz, hx, hy, hz, dn);
-    mixed_range<TPL>(tile, jneg, count, t, px, py, pz, hx, hy, hz, dp);
+    float dn = 3.0e38f, unused = 0;
+    mixed_range<TPL, true>(tile, 0, jneg, t, px, py, pz, hx, hy, hz, dn, l2);
+    mixed_range<TPL, false>(tile, jneg, count, t, px, py, pz, hx, hy, hz, unused, l2);
     dneg = fminf(dneg, dn);
-    dall = fminf(dall, fminf(dn, dp));
 }
 
 // FP64 field at (px, py, pz) from the staged records in global memory, lane
@@ -404,7 +409,8 @@ __device__ __forceinline__ void combine_group(int tg, T &ax, T &ay, T &az, T &dn
         ax = (T)__fadd_rn(hx.h, hx.l);                                                         \
         ay = (T)__fadd_rn(hy.h, hy.l);                                                         \
         az = (T)__fadd_rn(hz.h, hz.l);                                                         \
-        dall = group_min<float, G>(dall);                                                      \
+        if constexpr (MODE == EXT_MIXED)                                                       \
+            dall = group_sum<float, G>(dall);                                                  \
     } else {                                                                                   \
         ax = group_sum<T, G>(ax);                                                              \
         ay = group_sum<T, G>(ay);                                                              \

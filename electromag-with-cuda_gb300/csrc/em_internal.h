@@ -96,12 +96,13 @@ template <class T> struct ExtParams {
     const int *steps_per_line;      // optional per-line limits
     double resolution;
     double term_r2;
-    double null_frac;
+    double null_frac;               // (the call's option; the test uses kappa2)
     int *len, *cls;
     unsigned long long *next_line, *evals, *refines;
     int p_pad, n_tiles, tile_recs, stages, resident;
     int regroup;                    // widen lane groups once the queue is dry
-    int refine_df64;                // mixed: re-evaluate nulls in double-float
+    int refine_fp64;                // mixed: re-evaluate in FP64 (else double-float)
+    double kappa2;                  // mixed: the conditioning test's kappa^2
     int *err;
     // Tail hand-off.  Once the queue is dry and at most tail_lines lines are
     // still being traced, a kernel saves each of them (ExtCont) and stops;

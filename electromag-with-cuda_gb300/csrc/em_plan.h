@@ -17,6 +17,18 @@ constexpr int kMaxDevices = 64;
 // exceeds this multiple of |E| (the FP32 sum's error grows with it).
 constexpr double kMixKappaDefault = 2.5;
 
+// The conditioning bound of a call: refine_kappa when given, else
+// 1/null_frac when given (re-evaluate where |E| is below that fraction of
+// the terms' size), else the default.
+inline double mix_kappa(const em_options &o)
+{
+    if (o.refine_kappa > 0)
+        return o.refine_kappa;
+    if (o.null_frac > 0)
+        return 1.0 / o.null_frac;
+    return kMixKappaDefault;
+}
+
 // Cached per-device state.  `mu` serialises calls on one device; buffers
 // only grow and are released by em_release().
 struct DevCtx {

@@ -25,9 +25,9 @@
 //              inv^3 (s = s0 (2.5 - 1.5 r^2 inv^2), removing the rsqrt error
 //              to first order), two-sum compensated accumulation across
 //              chunks of 64 charges and across lanes, the line position in
-//              FP64, and an FP64 re-evaluation of the whole field where
-//              |E| < null_frac * (largest single contribution bound)
-//              (in double-float instead with refine_df64).
+//              FP64, and a double-float (or, with refine_fp64, FP64)
+//              re-evaluation of the whole field where the sum is
+//              ill-conditioned: sum_j |t_j|^2 > kappa^2 |E|^2.
 //   EXT_DF64   T = float: double-float pairs (two FP32 words each, about
 //              48 bits; the FP32 vertex makes r = p - c exact), compensated
 //              sums, the field and the step in FP64, the position in FP64:
@@ -44,7 +44,7 @@ namespace {
 // Staging: stable partition of p raw records into
 //   [negatives | pad to gran][positives | pad to p_pad], one CTA of 1024.
 // meta[0] = size of the padded negative block (records).
-// qabs[0] = largest |q| (float), for the mixed mode's contribution bound.
+// qabs[0] = largest |q| (float).
 template <class T>
 __global__ void __launch_bounds__(1024)
     ext_stage_kernel(const T *raw, int p, T *staged, int p_pad, int gran, int *meta, float *qabs)
@@ -125,6 +125,17 @@ __device__ __forceinline__ void ext_field(T &ax, T &ay, T &az, const CF &hx, con
         ay = (T)Edy;
         az = (T)Edz;
     }
+}
+
+// The mixed mode's test of the FP32 sum's conditioning: l2 = sum_j q_j^2 /
+// r_j^4 (no Coulomb constant), (ax, ay, az) the field with it; true where
+// sqrt(l2) K > kappa |E|.
+template <class T>
+__device__ __forceinline__ bool ext_ill_conditioned(const ExtParams<T> &P, float l2, T ax, T ay,
+                                                    T az)
+{
+    const double e2 = (double)ax * ax + (double)ay * ay + (double)az * az;
+    return (double)l2 * (kElectroK * kElectroK) > P.kappa2 * e2;
 }
 
 // One vertex of a live line once its field is known: the field store, the
@@ -225,7 +236,6 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
     }
     __syncthreads();
     const int jneg_all = *P.meta; // padded negative block (records)
-    const float qabs_max = *P.qabs; // largest |q|
 
     if (!streamed) {
         if (threadIdx.x == 0) {
@@ -413,7 +423,7 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         }
         // ---- field (and nearest negative charge) at the current vertex -----
         T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
-        float dall = 3.0e38f;
+        float dall = 0.0f; // mixed: sum of q^2/r^4 over the pairs
         CF hx, hy, hz;
         if (!streamed) {
             tile_pairs<T, MODE>(tg, tiles, jneg_all, P.p_pad, t, st, ax, ay, az, dneg, dall, hx,
@@ -452,16 +462,13 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
         ext_field<T, MODE>(ax, ay, az, hx, hy, hz, Edx, Edy, Edz);
 
         if constexpr (MODE == EXT_MIXED) {
-            // near a null |E| is far below its largest term and the FP32 sum
-            // loses its digits: redo the field in FP64 there (or in
-            // double-float, on the FP32 pipes, with refine_df64)
-            const float bound = qabs_max * (float)kElectroK / dall;
-            const float e2 = ax * ax + ay * ay + az * az;
-            const float lim2 = (float)P.null_frac * bound;
-            const bool redo = live && !(e2 >= lim2 * lim2);
+            // the FP32 sum's error grows with the size of its terms: where
+            // sum |t_j|^2 > kappa^2 |E|^2 (cancellation, nulls) redo the field
+            // in double-float (on the FP32 pipes) or, with refine_fp64, FP64
+            const bool redo = live && ext_ill_conditioned(P, dall, ax, ay, az);
             if (__any_sync(0xffffffffu, redo)) {
                 double fx = 0, fy = 0, fz = 0;
-                if (P.refine_df64)
+                if (!P.refine_fp64)
                     df64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
                                      (float)st.px, (float)st.py, (float)st.pz, fx, fy, fz,
                                      redo);
@@ -580,7 +587,6 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
     }
     __syncthreads();
     const int jneg_all = *P.meta;
-    const float qabs_max = *P.qabs;
     const long long count = (long long)*P.cont_in_count;
     const ExtCont<T> *cont = static_cast<const ExtCont<T> *>(P.cont_in);
     __shared__ unsigned long long sh_live;
@@ -730,7 +736,7 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
             r0z = ld_seed(P.z + line);
         }
         T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
-        float dall = 3.0e38f;
+        float dall = 0.0f; // mixed: sum of q^2/r^4 over the pairs
         CF hx, hy, hz;
         if (!streamed) {
             const int jn = min(max(jneg_all - pb, 0), pe - pb);
@@ -762,7 +768,8 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
             group_two_sum<32>(hx);
             group_two_sum<32>(hy);
             group_two_sum<32>(hz);
-            dall = group_min<float, 32>(dall);
+            if constexpr (MODE == EXT_MIXED)
+                dall = group_sum<float, 32>(dall);
         } else {
             ax = group_sum<T, 32>(ax);
             ay = group_sum<T, 32>(ay);
@@ -811,7 +818,8 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
                 ax = (T)__fadd_rn(hx.h, hx.l);
                 ay = (T)__fadd_rn(hy.h, hy.l);
                 az = (T)__fadd_rn(hz.h, hz.l);
-                dall = group_min<float, 32>(mine ? (float)gs[7] : 3.0e38f);
+                if constexpr (MODE == EXT_MIXED)
+                    dall = group_sum<float, 32>(mine ? (float)gs[7] : 0.0f);
             } else {
                 ax = group_sum<T, 32>(mine ? gs[0] : T(0));
                 ay = group_sum<T, 32>(mine ? gs[1] : T(0));
@@ -820,24 +828,21 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
             dneg = group_min<T, 32>(mine ? gs[6] : T(3.0e38));
             ext_field<T, MODE>(ax, ay, az, hx, hy, hz, Edx, Edy, Edz);
             if constexpr (MODE == EXT_MIXED) {
-                const float bound = qabs_max * (float)kElectroK / dall;
-                const float e2 = ax * ax + ay * ay + az * az;
-                const float lim2 = (float)P.null_frac * bound;
-                redo = live && !(e2 >= lim2 * lim2);
+                redo = live && ext_ill_conditioned(P, dall, ax, ay, az);
                 if (lane == 0)
                     grp_flag[g] = redo ? 2 : 0;
             }
         }
         if constexpr (MODE == EXT_MIXED) {
-            // near a null: the group re-evaluates the field in FP64 (or
-            // double-float), each warp its W-th of the staged records
+            // an ill-conditioned sum: the group re-evaluates the field in
+            // double-float (or FP64), each warp its W-th of the staged records
             if (__syncthreads_or(redo)) {
                 const bool gredo = grp_flag[g] == 2;
                 double fx = 0, fy = 0, fz = 0;
                 if (gredo) {
                     const int cb = pb, ce = pe;
                     const float4 *cr = reinterpret_cast<const float4 *>(P.charges) + cb;
-                    if (P.refine_df64)
+                    if (!P.refine_fp64)
                         field_df64<32>(cr, ce - cb, lane, (float)st.px, (float)st.py,
                                        (float)st.pz, fx, fy, fz);
                     else

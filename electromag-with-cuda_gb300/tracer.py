@@ -56,7 +56,7 @@ def calc_field(x, y, z, charges, n, resolution=1.0, use_curvature=True, *,
     sequence) or "mixed" (float32 only: compensated FP32 pairs with a
     Newton-corrected inv^3, the position in FP64, the field re-evaluated in
     double-float where sqrt(sum |t_j|^2) exceeds refine_kappa (default
-    2.5) times |E|).
+    2.5; refine_kappa 0 and null_frac > 0: 1/null_frac) times |E|).
 
     rc is the reference's code (0 ok, 1 n == 0, 2 resolution == 0,
     3 total_steps < 2, 5 n % 64 with require_n64) or a library code >= 4.
@@ -190,13 +190,15 @@ def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
                 steps_per_line=None, precision="fp32", want_field=False,
                 threads_per_line=0, warps_per_cta=0, tile_charges=0,
                 force_streamed=False, null_frac=0.0, deterministic=False,
-                refine="fp64", stream=None):
+                refine="df64", refine_kappa=0.0, stream=None):
     """Extended method (seeded lines, termination, step limits).
 
     seeds (n, 3), charges (p, 4): numpy arrays (host entry point) or CUDA
     torch tensors (device entry point, current stream).  precision: "fp32",
-    "mixed" (FP32 pairs, FP64 positions and near-null fields; refine: the
-    arithmetic of those re-evaluations, "fp64" or "df64"), "df64"
+    "mixed" (FP32 pairs, FP64 positions, and the field re-evaluated where
+    the sum is ill-conditioned, sqrt(sum |t_j|^2) > refine_kappa |E|
+    (default 2.5; refine_kappa 0 and null_frac > 0: 1/null_frac); refine:
+    the arithmetic of those re-evaluations, "df64" or "fp64"), "df64"
     (double-float pairs on the FP32 pipes, FP64 field and positions) or
     "fp64".
     Returns a dict with vertices (3, max_steps, n), len (n,), cls (n,),
@@ -212,6 +214,7 @@ def trace_lines(seeds, charges, max_steps, resolution=1.0, term_radius=0.5, *,
     o.tile_charges = tile_charges
     o.force_streamed = int(bool(force_streamed))
     o.null_frac = null_frac
+    o.refine_kappa = refine_kappa
     o.deterministic = int(bool(deterministic))
     o.refine = _REFINE[refine]
     perf = _capi.EmPerf()

@@ -102,9 +102,11 @@ typedef struct em_options {
     int lines_per_thread; /* 0: automatic; 1 or 2 (fast arithmetic only)     */
     int precision;        /* em_trace_lines_f32: EM_PREC_FP32, EM_PREC_MIXED
                              or EM_PREC_DF64                                 */
-    double null_frac;     /* mixed: FP64 re-evaluation where |E| is below this
-                             fraction of the largest single contribution
-                             (0: 1e-4)                                       */
+    double null_frac;     /* mixed (both tracers), when refine_kappa is 0:
+                             re-evaluate the field where |E| is below this
+                             fraction of the terms' size sqrt(sum |t_j|^2),
+                             i.e. refine_kappa = 1/null_frac (0: the
+                             default 2.5 of refine_kappa)                    */
     int deterministic;    /* extended tracer: 1 keeps every line on its
                              initial lane group, so results repeat bit for
                              bit; 0 (default) lets warps widen the groups of
@@ -115,33 +117,33 @@ typedef struct em_options {
                              field at every vertex (12 more bytes per vertex);
                              1 keeps only the vertices and recomputes the
                              field per 64-row segment                        */
-    int refine;           /* mixed precision: EM_REFINE_FP64 (default) or
-                             EM_REFINE_DF64, the arithmetic of the field
-                             re-evaluated near nulls                         */
+    int refine;           /* em_trace_lines_f32, mixed precision:
+                             EM_REFINE_DF64 (default) or EM_REFINE_FP64, the
+                             arithmetic of the re-evaluated field            */
     void *field_out;      /* em_calc_field_ex_* with device_ptrs only
                              (NULL: none): the field each step uses, as the
                              arrays' type, Coulomb constant applied; three
                              arrays of n*(total_steps-1) values back to back
                              (x, then y, then z), the field at vertex s of
                              line l at s*n + l                               */
-    double refine_kappa;  /* EM_ARITH_MIXED, em_calc_field_ex_f32: a vertex's
-                             field is re-evaluated in double-float where the
-                             terms' size sqrt(sum_j |t_j|^2) (estimated from
-                             the compensated chunk sums) exceeds
-                             refine_kappa * |E| (0: 2.5)                     */
+    double refine_kappa;  /* mixed arithmetic (EM_ARITH_MIXED on the
+                             reference loop, EM_PREC_MIXED in the extended
+                             tracer): a vertex's field is re-evaluated where
+                             the terms' size sqrt(sum_j |t_j|^2) exceeds
+                             refine_kappa * |E| (0: see null_frac)           */
 } em_options;
 
 /* ---- precision of the extended tracer (em_trace_lines_f32) ---------------- */
 #define EM_PREC_FP32 0    /* FP32 pairs and positions                        */
 #define EM_PREC_MIXED 1   /* FP32 pairs with a Newton-corrected inv^3,
-                             compensated sums, FP64 positions, FP64 field
-                             near nulls                                      */
+                             compensated sums, FP64 positions, the field
+                             re-evaluated where the sum is ill-conditioned   */
 #define EM_PREC_DF64 2    /* double-float pairs (two FP32 words, ~48 bits) on
                              the FP32 pipes, FP64 field, step and positions:
                              FP64-class fields at several times the native
                              FP64 rate of GB300                              */
-#define EM_REFINE_FP64 0  /* mixed: re-evaluate near nulls in FP64           */
-#define EM_REFINE_DF64 1  /* mixed: re-evaluate near nulls in double-float   */
+#define EM_REFINE_DF64 0  /* mixed: re-evaluate in double-float (default)    */
+#define EM_REFINE_FP64 1  /* mixed: re-evaluate in FP64                      */
 
 /* ---- termination classes of the extended tracer --------------------------- */
 #define EM_TERM_STEPS 0   /* reached its step limit                          */

@@ -139,7 +139,9 @@ def test_extended_all_positive_charges_never_hit(em, gpu):
 
 def test_mixed_field_error_vs_fp64(em, gpu, orc, ext_case):
     """Mixed precision: the field the kernel used at each vertex against the
-    FP64 field at that same (FP32) point."""
+    FP64 field at that same (FP32) point — within 1e-6 at every vertex (the
+    conditioning test re-evaluates the ill-conditioned ones), and without the
+    re-evaluations not."""
     ch, seeds, steps, _ = ext_case
     out = em.trace_lines(seeds, ch, 200, 1.0, 0.5, precision="mixed",
                          want_field=True)
@@ -153,8 +155,9 @@ def test_mixed_field_error_vs_fp64(em, gpu, orc, ext_case):
     fld = np.concatenate(fld).astype(np.float64)
     e64 = orc.field_f64(pts, ch.astype(np.float64))
     rel = np.linalg.norm(fld - e64, axis=1) / np.linalg.norm(e64, axis=1)
-    assert np.median(rel) <= 1e-6, np.median(rel)
-    assert np.quantile(rel, 0.999) <= 1e-5, np.quantile(rel, 0.999)
+    assert np.median(rel) <= 2e-7, np.median(rel)
+    assert rel.max() <= 1e-6, (rel.max(), (rel > 1e-6).sum())
+    assert out["perf"].fp64_refines > 0
 
 
 def test_regrouping_tail_agrees_and_is_faster(em, gpu, orc):
@@ -256,7 +259,8 @@ def test_df64_matches_fp64_oracle(em, gpu, ext_case):
 
 
 def test_mixed_refinement_in_df64_equals_fp64(em, gpu, ext_case):
-    """Every vertex re-evaluated (null_frac far above 1): the double-float
+    """Every vertex re-evaluated (null_frac far above 1, a conditioning
+    bound of 1e-30): the double-float
     and FP64 re-evaluations round to the same FP32 field almost everywhere
     and never differ by more than one rounding."""
     ch, seeds, _, _ = ext_case
