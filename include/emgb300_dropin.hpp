@@ -14,7 +14,10 @@
 #ifndef EMGB300_DROPIN_HPP
 #define EMGB300_DROPIN_HPP
 
+#include <atomic>
+#include <chrono>
 #include <cstddef>
+#include <thread>
 #include <vector>
 
 #include "emgb300.h"
@@ -38,6 +41,10 @@ inline int call(double *x, double *y, double *z, size_t n, size_t steps, const v
 // useCurvature) over the reference's SoA container (Vector3<Array<T>>).
 // totalSteps = fieldLines.GetSize()/n as in CPU_Implement.cpp:219; the
 // n == 0 check precedes the division like the reference's.
+// perfData.progress follows the call's progress while it runs (a watcher
+// thread copies em_perf.progress every millisecond), so a monitor thread
+// polling it, as the reference's does ("Electromag utils.h":133-156), sees
+// the rows traced so far.
 template <class T, class Lines, class Charges, class Perf>
 int calc_field(Lines &fieldLines, Charges &pointCharges, size_t n, T resolution,
                Perf &perfData, bool useCurvature)
@@ -45,9 +52,20 @@ int calc_field(Lines &fieldLines, Charges &pointCharges, size_t n, T resolution,
     em_perf ep = em_perf();
     const size_t steps = n ? fieldLines.GetSize() / n : 0;
     auto d = fieldLines.GetDataPointers();
+    std::atomic<bool> done(false);
+    std::thread watcher([&] {
+        while (!done.load(std::memory_order_acquire)) {
+            const double v = ep.progress;
+            if (v > 0 && v < 1)
+                perfData.progress = v;
+            std::this_thread::sleep_for(std::chrono::milliseconds(1));
+        }
+    });
     const int rc = call(d.x, d.y, d.z, n, steps,
                         static_cast<const void *>(pointCharges.GetDataPointer()),
                         pointCharges.GetSize(), resolution, useCurvature, &ep);
+    done.store(true, std::memory_order_release);
+    watcher.join();
     if (rc == EM_OK) {
         perfData.time = ep.time;
         perfData.performance = ep.performance;
