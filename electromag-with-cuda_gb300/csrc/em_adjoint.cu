@@ -434,27 +434,51 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
 }
 
 // Adds a lane's register sums into its team's compensated partials and
-// clears them; lane l of warp wt owns records (k*W + wt)*32 + l.
+// clears them; lane l of warp wt owns records (k*W + wt)*32 + l, its sums
+// held as packed pairs (k = 2kp in the low half, 2kp + 1 in the high half).
 template <int CPL, int W>
 __device__ __forceinline__ void adj_flush(const AdjParams &P, long long team, int wt, int lane,
-                                          float (&g)[4][CPL])
+                                          u64 (&g)[4][CPL / 2])
 {
     constexpr int PB = 32 * W * CPL;
     float2 *tp = P.tpart + (size_t)team * 4 * PB + wt * 32 + lane;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
 #pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-            float2 *q = tp + c * PB + k * W * 32;
-            float2 v = *q;
-            float sum, err;
-            two_sum_f(v.x, g[c][k], sum, err);
-            v.x = sum;
-            v.y = __fadd_rn(v.y, err);
-            *q = v;
-            g[c][k] = 0.0f;
+        for (int kp = 0; kp < CPL / 2; ++kp) {
+            float gv[2];
+            f2_unpack(g[c][kp], gv[0], gv[1]);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float2 *q = tp + c * PB + (2 * kp + h) * W * 32;
+                float2 v = *q;
+                float sum, err;
+                two_sum_f(v.x, gv[h], sum, err);
+                v.x = sum;
+                v.y = __fadd_rn(v.y, err);
+                *q = v;
+            }
+            g[c][kp] = 0ull;
         }
     }
+}
+
+// The fused backward's records in lane pairs: slot (kp*W + wt)*32 + l of
+// the A plane holds {x, x', y, y'} and of the B plane {z, z', q, q'} for the
+// lane's charges k = 2kp and 2kp + 1 (plain records (k*W + wt)*32 + l), so
+// each pair of them feeds one packed instruction.
+__global__ void adj_pair_stage_kernel(const float4 *plain, int p_bwd, int W, float4 *paired)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int half = p_bwd / 2;
+    if (i >= half)
+        return;
+    const int l = i & 31, rest = i >> 5;
+    const int kp = rest / W, wt = rest - kp * W;
+    const float4 a = plain[((2 * kp) * W + wt) * 32 + l];
+    const float4 b = plain[((2 * kp + 1) * W + wt) * 32 + l];
+    paired[i] = make_float4(a.x, b.x, a.y, b.y);
+    paired[half + i] = make_float4(a.z, b.z, a.w, b.w);
 }
 
 // Fused backward over rows [s_lo, s_hi) of every line (see the file
@@ -469,8 +493,10 @@ __global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     float4 *red = reinterpret_cast<float4 *>(smem + 128); // [2 parities][4 warps]
-    const float4 *ch = reinterpret_cast<const float4 *>(smem + 256) + wt_of(threadIdx.x, W) * 32 +
-                       (threadIdx.x & 31);
+    // the lane's charge pairs: A plane {x, x', y, y'}, B plane {z, z', q, q'}
+    const ulonglong2 *chA = reinterpret_cast<const ulonglong2 *>(smem + 256) +
+                            wt_of(threadIdx.x, W) * 32 + (threadIdx.x & 31);
+    const ulonglong2 *chB = chA + 16 * W * CPL;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tpc = (int)(blockDim.x >> 5) / W;
     const int team = warp / W, wt = warp - team * W;
@@ -483,7 +509,7 @@ __global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const
     if (threadIdx.x == 0) {
         const uint32_t bytes = (uint32_t)P.p_bwd * 16u;
         mbar_arrive_expect_tx(b0, bytes);
-        const char *src = static_cast<const char *>(P.charges);
+        const char *src = static_cast<const char *>(P.charges_bwd);
         constexpr uint32_t CHUNK = 32768;
         const uint32_t dst = smem_addr(smem + 256);
         for (uint32_t off = 0; off < bytes; off += CHUNK)
@@ -500,12 +526,13 @@ __global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const
     const float K = (float)kElectroK;
     const unsigned FULL = 0xffffffffu;
 
-    float g[4][CPL]; // x, y, z gradient sums and -3 sum r.mu/r^3 per owned charge
+    // x, y, z gradient sums and -3 sum r.mu/r^3 per owned charge, in pairs
+    u64 g[4][CPL / 2];
 #pragma unroll
     for (int c = 0; c < 4; ++c)
 #pragma unroll
-        for (int k = 0; k < CPL; ++k)
-            g[c][k] = 0.0f;
+        for (int kp = 0; kp < CPL / 2; ++kp)
+            g[c][kp] = 0ull;
     int acc_rows = 0;
 
     for (long long line = tid; line < P.n; line += nteams) {
@@ -564,27 +591,43 @@ __global__ void __launch_bounds__(128, CPL >= 32 ? 2 : 3) adj_fused_kernel(const
                 const float m3x = -3.0f * mx, m3y = -3.0f * my, m3z = -3.0f * mz;
                 // G(r) mu = inv3 h, h = mu + (d3 inv2) r with d3 = -3 r.mu:
                 // h feeds the charge's position sums and, times q inv3, the
-                // line's Jacobian-vector sum l
-                float lx = 0, ly = 0, lz = 0;
+                // line's Jacobian-vector sum l; two charges per packed
+                // instruction
+                const u64 VX = f2_pack(vx, vx), VY = f2_pack(vy, vy), VZ = f2_pack(vz, vz);
+                const u64 MX = f2_pack(mx, mx), MY = f2_pack(my, my), MZ = f2_pack(mz, mz);
+                const u64 NX = f2_pack(m3x, m3x), NY = f2_pack(m3y, m3y),
+                          NZ = f2_pack(m3z, m3z);
+                u64 LX = 0ull, LY = 0ull, LZ = 0ull;
 #pragma unroll
-                for (int k = 0; k < CPL; ++k) {
-                    const float4 c = ch[k * W * 32];
-                    const float dx = vx - c.x, dy = vy - c.y, dz = vz - c.z;
-                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    const float inv = rsqrt_fast(r2);
-                    const float inv2 = inv * inv;
-                    const float inv3 = inv2 * inv;
-                    const float d3 = fmaf(dz, m3z, fmaf(dy, m3y, dx * m3x));
-                    const float t = d3 * inv2;
-                    const float hx = fmaf(t, dx, mx), hy = fmaf(t, dy, my), hz = fmaf(t, dz, mz);
-                    g[0][k] = fmaf(inv3, hx, g[0][k]);
-                    g[1][k] = fmaf(inv3, hy, g[1][k]);
-                    g[2][k] = fmaf(inv3, hz, g[2][k]);
-                    g[3][k] = fmaf(d3, inv3, g[3][k]);
-                    const float qi3 = c.w * inv3;
-                    lx = fmaf(qi3, hx, lx);
-                    ly = fmaf(qi3, hy, ly);
-                    lz = fmaf(qi3, hz, lz);
+                for (int kp = 0; kp < CPL / 2; ++kp) {
+                    const ulonglong2 A = chA[kp * W * 32], B = chB[kp * W * 32];
+                    const u64 dx = f2_sub(VX, A.x), dy = f2_sub(VY, A.y), dz = f2_sub(VZ, B.x);
+                    const u64 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+                    const u64 inv = f2_rsqrt(r2);
+                    const u64 inv2 = f2_mul(inv, inv);
+                    const u64 inv3 = f2_mul(inv2, inv);
+                    const u64 d3 = f2_fma(dz, NZ, f2_fma(dy, NY, f2_mul(dx, NX)));
+                    const u64 t = f2_mul(d3, inv2);
+                    const u64 hx = f2_fma(t, dx, MX), hy = f2_fma(t, dy, MY),
+                              hz = f2_fma(t, dz, MZ);
+                    g[0][kp] = f2_fma(inv3, hx, g[0][kp]);
+                    g[1][kp] = f2_fma(inv3, hy, g[1][kp]);
+                    g[2][kp] = f2_fma(inv3, hz, g[2][kp]);
+                    g[3][kp] = f2_fma(d3, inv3, g[3][kp]);
+                    const u64 qi3 = f2_mul(B.y, inv3);
+                    LX = f2_fma(qi3, hx, LX);
+                    LY = f2_fma(qi3, hy, LY);
+                    LZ = f2_fma(qi3, hz, LZ);
+                }
+                float lx, ly, lz;
+                {
+                    float a, b;
+                    f2_unpack(LX, a, b);
+                    lx = a + b;
+                    f2_unpack(LY, a, b);
+                    ly = a + b;
+                    f2_unpack(LZ, a, b);
+                    lz = a + b;
                 }
                 // warp sums of (lx, ly, lz): halve the values a lane carries
                 // at offsets 16 and 8 (each lane sends the half its partner
@@ -777,6 +820,18 @@ cudaError_t launch_fused(const AdjParams &P, const AdjFused &f, int lo, int hi,
 }
 
 } // namespace
+
+cudaError_t launch_adjoint_pair_stage(const void *plain, int p_bwd, int team_warps,
+                                      void *paired, cudaStream_t stream)
+{
+    const int half = p_bwd / 2;
+    if (half <= 0)
+        return cudaErrorInvalidValue;
+    adj_pair_stage_kernel<<<(half + 255) / 256, 256, 0, stream>>>(
+        static_cast<const float4 *>(plain), p_bwd, team_warps, static_cast<float4 *>(paired));
+    count_launch(1);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, int nsm,
                                     size_t smem, double *loss, double *grad,

@@ -62,7 +62,9 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     cudaStream_t s = (o.device_ptrs && o.stream) ? (cudaStream_t)o.stream : c.stream;
     const int p_stage = fused ? std::max(pl.p_pad, af.p_bwd) : pl.p_pad;
 
-    if ((code = grow(&c.charges, &c.charges_cap, (size_t)p_stage * 16)))
+    // the fused backward's lane-pair copy of the records follows the plain ones
+    if ((code = grow(&c.charges, &c.charges_cap,
+                     (size_t)(p_stage + (fused ? af.p_bwd : 0)) * 16)))
         return code;
     if ((code = grow(&c.charges_raw, &c.charges_raw_cap, p * 16 + 16)))
         return code;
@@ -118,6 +120,9 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
     if (e == cudaSuccess)
         e = launch_stage_charges<float>(c.charges_raw, (int)p, c.charges, p_stage, 0,
                                         pl.cfg.tile_recs, s);
+    void *paired = static_cast<float4 *>(c.charges) + p_stage;
+    if (e == cudaSuccess && fused)
+        e = launch_adjoint_pair_stage(c.charges, af.p_bwd, af.team_warps, paired, s);
     if (e == cudaSuccess && !o.device_ptrs) {
         const float *src[6] = {x, y, z, tx, ty, tz};
         float *dst[6] = {dx, dy, dz, const_cast<float *>(dtx), const_cast<float *>(dty),
@@ -185,6 +190,7 @@ int adjoint(float *x, float *y, float *z, size_t n, size_t rows, const float *ch
         ap.stored = stored ? 1 : 0;
         ap.tpart = reinterpret_cast<float2 *>(ws + off_tpart);
         ap.p_bwd = af.p_bwd;
+        ap.charges_bwd = paired;
         ap.team_warps = af.team_warps;
         ap.teams = af.teams;
     }

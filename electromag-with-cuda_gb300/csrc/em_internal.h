@@ -167,6 +167,7 @@ struct AdjParams {
     float2 *tpart;
     int p_bwd, team_warps;
     long long teams;
+    const void *charges_bwd;   // fused backward: the records in lane pairs
 };
 // Shape of the fused backward (p up to kAdjFusedMaxCharges charges).
 constexpr int kAdjFusedMaxCharges = 4096;
@@ -188,6 +189,9 @@ int adjoint_fused_plan(int p, int nsm, AdjFused *f);
 // Checkpoint mode (fused, field not stored): the field of segment k is
 // recomputed on `side` into half k % 2 of a two-segment buffer (half_elems
 // apart) while the fused kernel of segment k - 1 runs on `stream`.
+// The fused backward's lane-pair layout of p_bwd staged plain records.
+cudaError_t launch_adjoint_pair_stage(const void *plain, int p_bwd, int team_warps,
+                                      void *paired, cudaStream_t stream);
 cudaError_t launch_adjoint_backward(const AdjParams &P, const AdjFused *fused, int nsm,
                                     size_t smem, double *loss, double *grad,
                                     cudaStream_t stream, cudaStream_t side,
