@@ -466,22 +466,32 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
             // sum |t_j|^2 > kappa^2 |E|^2 (cancellation, nulls) redo the field
             // in double-float (on the FP32 pipes) or, with refine_fp64, FP64
             const bool redo = live && ext_ill_conditioned(P, dall, ax, ay, az);
-            if (__any_sync(0xffffffffu, redo)) {
+            // each flagged vertex in turn, its field split over the whole
+            // warp (records from shared memory when resident)
+            unsigned m = __ballot_sync(0xffffffffu, redo && t == 0);
+            const float4 *rec = streamed ? reinterpret_cast<const float4 *>(P.charges)
+                                         : reinterpret_cast<const float4 *>(tiles);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const float rx = __shfl_sync(0xffffffffu, (float)st.px, src);
+                const float ry = __shfl_sync(0xffffffffu, (float)st.py, src);
+                const float rz = __shfl_sync(0xffffffffu, (float)st.pz, src);
                 double fx = 0, fy = 0, fz = 0;
                 if (!P.refine_fp64)
-                    df64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad, t,
-                                     (float)st.px, (float)st.py, (float)st.pz, fx, fy, fz,
-                                     redo);
+                    field_df64<32>(rec, P.p_pad, lane, rx, ry, rz, fx, fy, fz);
                 else
-                    fp64_field_group(tg, reinterpret_cast<const float4 *>(P.charges), P.p_pad,
-                                     t, (double)(float)st.px, (double)(float)st.py,
-                                     (double)(float)st.pz, fx, fy, fz, redo);
-                if (redo) {
+                    field_fp64<32>(rec, P.p_pad, lane, (double)rx, (double)ry, (double)rz, fx,
+                                   fy, fz);
+                fx = group_sum<double, 32>(fx);
+                fy = group_sum<double, 32>(fy);
+                fz = group_sum<double, 32>(fz);
+                if (lane / tg == src / tg) {
                     ax = (T)(fx * kElectroK);
                     ay = (T)(fy * kElectroK);
                     az = (T)(fz * kElectroK);
-                    refines += (t == 0);
                 }
+                refines += (lane == src);
             }
         }
         // tail hand-off: with the queue dry, once few enough lines are left
