@@ -60,7 +60,7 @@ def parse():
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
     ap.add_argument("--case", choices=["ref-mixed", "ext-fp32", "ext-mixed", "ext-df64",
-                                       "ext-tail-dipole", "adjoint",
+                                       "ext-tail-dipole", "ext-tail-gpu", "adjoint",
                                        "adjoint-checkpoint", "adjoint-twopass",
                                        "batch", "verlet"],
                     default=None,
@@ -232,7 +232,9 @@ def run_case(args):
     reference-layout tracer (4096 charges, 200 rows), the extended kernel on the
     4096-charge workload (200 rows, no termination radius; FP32, mixed or
     double-float pairs), the extended tracer with its tail kernel on the
-    dipole set (1000 rows, termination radius 0.5), the adjoint
+    dipole set (1000 rows, termination radius 0.5) or on the 4096-charge
+    workload (5000 rows, termination radius 0.5: lines that escape the
+    charges run all rows, on the tail kernel), the adjoint
     kernels on the 1024-charge workload (200 rows; stored field, or the
     field recomputed per 64-row segment; adjoint-twopass: 6000 charges, the
     two-pass backward of sets above 4096 charges), the batched tracer on the
@@ -282,6 +284,18 @@ def run_case(args):
         out = em.trace_lines(s, ch, 1000, 1.0, 0.5)
         torch.cuda.synchronize()
         print("tail", out["perf"].pairs / out["perf"].time / 1e9, "Gpair/s")
+        return 0
+    if args.case == "ext-tail-gpu":
+        ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)
+        ch = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).to(dev)
+        s = torch.from_numpy(seeds.astype(np.float32)).to(dev)
+        rows = args.rows or 5000
+        out = em.trace_lines(s, ch, rows, 1.0, 0.5)
+        torch.cuda.synchronize()
+        ln = out["len"]
+        print("tail", out["perf"].pairs / out["perf"].time / 1e9, "Gpair/s",
+              out["perf"].time * 1e3, "ms, lines at the row limit",
+              int((ln >= rows).sum()))
         return 0
     if args.case.startswith("ext"):
         ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)

@@ -83,6 +83,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     cfg.tpl = tpl;
     cfg.kl = 1;
     cfg.grid = c.nsm;
+    const int cta_warps = ext_cta_threads(mode) / 32;
     cfg.resident = !o.force_streamed && 128 + (size_t)p_min * rec <= smem_cap;
     int p_pad, n_tiles, tile;
     if (cfg.resident) {
@@ -90,7 +91,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
         n_tiles = 1;
         tile = p_pad;
         cfg.stages = 1;
-        cfg.warps = o.warps_per_cta ? std::min(o.warps_per_cta, 32) : 32;
+        cfg.warps = std::min(o.warps_per_cta ? o.warps_per_cta : 32, cta_warps);
         cfg.smem = 128 + (size_t)p_pad * rec;
     } else {
         tile = o.tile_charges ? o.tile_charges : (rec == 16 ? 1024 : 512);
@@ -107,7 +108,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             tile = (int)(ceil_div(ceil_div(p_min, n_tiles), gran) * gran);
         }
         p_pad = n_tiles * tile;
-        cfg.warps = o.warps_per_cta ? std::min(o.warps_per_cta, 31) : 31;
+        cfg.warps = std::min(o.warps_per_cta ? o.warps_per_cta : 31, cta_warps - 1);
         cfg.smem = 128 + (size_t)cfg.stages * tile * rec;
     }
     cfg.tile_recs = tile;
@@ -155,7 +156,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     // them.  With resident charges a lone line gains from more warps as
     // long as each warp keeps enough pairs per row (w_cap below).
     LaunchCfg wcfg = cfg;
-    wcfg.warps = cfg.resident ? 32 : 30;
+    wcfg.warps = kExtWideThreads / 32 - (cfg.resident ? 0 : 1);
     int wide_tiles = n_tiles;
     if (!cfg.resident) {
         // streamed: a wide group splits every tile W ways, so its warps

@@ -80,6 +80,13 @@ enum ExtMode : int {
     EXT_MIXED = 1, // FP32 pairs + corrected inv^3 + compensation, FP64 position
     EXT_DF64 = 2,  // double-float pairs (two FP32 words), FP64 position and step
 };
+// CTA size cap of the lane-group kernel: the mixed pass needs more than the
+// 64 registers a 1024-thread CTA leaves a thread (it spilled there)
+constexpr int ext_cta_threads(int mode) { return mode == EXT_MIXED ? 512 : 1024; }
+// CTA size of the tail kernel in every mode: its rows are a latency chain
+// (pairs, two reductions, the step), which the 128-register cap shortens
+// (GPU-scale set with termination, FP32: 12.1 ms at 1024 threads, 9.9 at 512)
+constexpr int kExtWideThreads = 512;
 // termination classes written by the kernel (same values as EM_TERM_*)
 constexpr int EM_TERM_STEPS_DEV = 0;
 constexpr int EM_TERM_CHARGE_DEV = 1;

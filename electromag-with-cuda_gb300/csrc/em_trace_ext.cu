@@ -208,7 +208,8 @@ __device__ __forceinline__ void live_count_drop(unsigned long long *c)
 }
 
 template <class T, int TPL, int MODE>
-__global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P)
+__global__ void __launch_bounds__(ext_cta_threads(MODE), 1)
+    ext_trace_kernel(const ExtParams<T> P)
 {
     using Rec = typename ChargeRec<T>::type;
     constexpr int LG = 32 / TPL; // line slots per warp
@@ -564,7 +565,7 @@ __global__ void __launch_bounds__(1024, 1) ext_trace_kernel(const ExtParams<T> P
 // which the other warps read after the row's last barrier.  A group whose
 // line ends takes the next handed-off line.
 template <class T, int MODE>
-__global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
+__global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtParams<T> P)
 {
     using Rec = typename ChargeRec<T>::type;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -942,11 +943,352 @@ __global__ void __launch_bounds__(1024, 1) ext_wide_kernel(const ExtParams<T> P)
     }
 }
 
+// Barrier over the nthreads threads (whole warps) of one line group; id 1..15
+// (0 is the CTA barrier).
+__device__ __forceinline__ void group_barrier(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// The handed-off lines with resident charges.  The same work as
+// ext_wide_kernel, but the groups of a CTA run independently and a row costs
+// one barrier, over the group only: each warp sums its W-th of the resident
+// records and puts its sums into the row's slots (two sets, by row parity);
+// after the barrier every warp of the group combines the W slots in the same
+// order and runs the vertex step itself, so all of them hold the same vertex
+// without a second exchange; warp 0, lane 0 of the group stores.  A group
+// takes another barrier only where it needs one as a whole: a re-evaluation
+// (mixed) and its next line's index.  The live-line count behind the
+// hand-off test is loaded one row before it is used, off the row's chain.
+template <class T, int MODE>
+__global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const ExtParams<T> P)
+{
+    using Rec = typename ChargeRec<T>::type;
+    constexpr int MW = kExtWideThreads / 32;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ T slots[2][MW][8];   // each warp's sums, by row parity
+    __shared__ double rslots[MW][4]; // each warp's re-evaluation sums
+    __shared__ long long grp_next[MW];
+    __shared__ unsigned long long grp_live[2][MW];
+    __shared__ T grp_pos[MW][3]; // the first warp's vertex after the step
+    __shared__ int grp_flag[MW];
+    // FP32 steps run in every warp of a group (no second exchange); steps
+    // with FP64 parts (mixed position, double-float, FP64) run on the
+    // group's first warp only: repeated in every warp they queue on the
+    // FP64 pipe (mixed 18.4 -> 25.8 ms, double-float 47 -> 95 ms)
+    constexpr bool kAllStep = MODE == EXT_FAST && sizeof(T) == 4;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    Rec *tiles = reinterpret_cast<Rec *>(smem + 128);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const int W = P.wide;
+    if (!P.resident || nwarps > MW || W < 1 || nwarps % W != 0) {
+        if (threadIdx.x == 0)
+            atomicCAS(P.err, 0, EM_DEVERR_CONFIG);
+        return;
+    }
+    const uint32_t full0 = smem_addr(bars);
+    if (threadIdx.x == 0) {
+        mbar_init(full0, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)P.p_pad * (uint32_t)sizeof(Rec);
+        mbar_arrive_expect_tx(full0, bytes);
+        const char *src = static_cast<const char *>(P.charges);
+        const uint32_t dst = smem_addr(tiles);
+        constexpr uint32_t CH = 32768;
+        for (uint32_t off = 0; off < bytes; off += CH)
+            bulk_g2s(dst + off, src + off, bytes - off < CH ? bytes - off : CH, full0);
+    }
+    // a wait that gave up anywhere stops the whole CTA before the groups part
+    if (__syncthreads_or(!mbar_wait(full0, 0, P.err)))
+        return;
+
+    const int jneg_all = *P.meta;
+    const long long count = (long long)*P.cont_in_count;
+    const ExtCont<T> *cont = static_cast<const ExtCont<T> *>(P.cont_in);
+    const int g = warp / W, wg = warp - g * W;
+    const int t = wg * 32 + lane; // thread index within the group
+    const int gthreads = 32 * W;
+    auto gsync = [&]() {
+        if (W == 1)
+            __syncwarp();
+        else
+            group_barrier(1 + g, gthreads);
+    };
+    long long line = -1;
+    int s = 1, lim = 0;
+    bool live = false;
+    ExtLane<T> st;
+    T r0x = 0, r0y = 0, r0z = 0;
+    auto take = [&]() {
+        const long long k = grp_next[g];
+        live = k < count;
+        if (live) {
+            const ExtCont<T> c = cont[k];
+            line = c.line;
+            s = c.s;
+            lim = c.lim;
+            st.px = c.px;
+            st.py = c.py;
+            st.pz = c.pz;
+            st.dx = c.dx;
+            st.dy = c.dy;
+            st.dz = c.dz;
+            r0x = ld_seed(P.x + line);
+            r0y = ld_seed(P.y + line);
+            r0z = ld_seed(P.z + line);
+        }
+    };
+    if (t == 0)
+        grp_next[g] = (long long)atomicAdd(P.cont_next, 1ull);
+    gsync();
+    take();
+
+    // this warp's W-th of the resident records, fixed for the launch
+    const int pb = (int)((long long)P.p_pad * wg / W);
+    const int pe = (int)((long long)P.p_pad * (wg + 1) / W);
+    const int jn = min(max(jneg_all - pb, 0), pe - pb);
+    const float4 *recs = reinterpret_cast<const float4 *>(tiles);
+
+    unsigned long long evals = 0, refines = 0, live_seen = ~0ull;
+    // the group's sums from the row's slots (lane w takes warp w's), in the
+    // same order in every warp
+    auto combine = [&](int par, T &ax, T &ay, T &az, T &dneg, float &dall, CF &hx, CF &hy,
+                       CF &hz, double &Edx, double &Edy, double &Edz) {
+        const bool mine = lane < W;
+        const T *gs = slots[par][g * W + (mine ? lane : 0)];
+        if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+            hx.h = mine ? gs[0] : 0.0f;
+            hx.l = mine ? gs[1] : 0.0f;
+            hy.h = mine ? gs[2] : 0.0f;
+            hy.l = mine ? gs[3] : 0.0f;
+            hz.h = mine ? gs[4] : 0.0f;
+            hz.l = mine ? gs[5] : 0.0f;
+            group_two_sum<32>(hx);
+            group_two_sum<32>(hy);
+            group_two_sum<32>(hz);
+            ax = (T)__fadd_rn(hx.h, hx.l);
+            ay = (T)__fadd_rn(hy.h, hy.l);
+            az = (T)__fadd_rn(hz.h, hz.l);
+            if constexpr (MODE == EXT_MIXED)
+                dall = group_sum<float, 32>(mine ? (float)gs[7] : 0.0f);
+        } else {
+            ax = group_sum<T, 32>(mine ? gs[0] : T(0));
+            ay = group_sum<T, 32>(mine ? gs[1] : T(0));
+            az = group_sum<T, 32>(mine ? gs[2] : T(0));
+        }
+        dneg = group_min<T, 32>(mine ? gs[6] : T(3.0e38));
+        ext_field<T, MODE>(ax, ay, az, hx, hy, hz, Edx, Edy, Edz);
+    };
+    // a finished line (t == 0): its length and class, the next line's index
+    auto finish = [&](int cls) {
+        P.len[line] = s;
+        P.cls[line] = cls;
+        if (P.tail_lines > 0)
+            live_count_drop(P.live_count);
+        grp_next[g] = (long long)atomicAdd(P.cont_next, 1ull);
+    };
+    // a line handed on to a wider launch (t == 0); every input line was
+    // taken at the start (a group each), so nothing is left behind
+    auto save = [&]() {
+        const unsigned long long k = atomicAdd(P.cont_count, 1ull);
+        ExtCont<T> c;
+        c.line = line;
+        c.s = s;
+        c.lim = lim;
+        c.px = st.px;
+        c.py = st.py;
+        c.pz = st.pz;
+        c.dx = st.dx;
+        c.dy = st.dy;
+        c.dz = st.dz;
+        static_cast<ExtCont<T> *>(P.cont)[k] = c;
+        live_count_drop(P.live_count);
+    };
+    // the first warp's vertex step: 1 the line goes on, 4 it ended and the
+    // next line's index is out, 0 it was handed on
+    auto step = [&](int par, bool use_row, T ax, T ay, T az, double Edx, double Edy,
+                    double Edz, T dneg) -> int {
+        const bool hand_off = use_row && grp_live[par][g] <= (unsigned long long)P.tail_lines;
+        evals += (t == 0);
+        const int cls = ext_vertex<T, MODE>(P, line, s, lim, st, t, ax, ay, az, Edx, Edy, Edz,
+                                            dneg, r0x, r0y, r0z);
+        if (cls >= 0) {
+            if (t == 0)
+                finish(cls);
+            return 4;
+        }
+        if (hand_off) {
+            if (t == 0)
+                save();
+            return 0;
+        }
+        return 1;
+    };
+    unsigned row_iter = 0;
+    while (live) {
+        const int par = row_iter & 1;
+        // every 8th row: the live-line count, loaded a row before its use
+        const bool load_row = P.tail_lines > 0 && (row_iter & 7) == 7;
+        const bool use_row = P.tail_lines > 0 && (row_iter & 7) == 0 && row_iter > 0;
+        ++row_iter;
+        if (t == 0 && load_row)
+            live_seen = *(volatile unsigned long long *)P.live_count;
+
+        T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
+        float dall = 0.0f; // mixed: sum of q^2/r^4 over the pairs
+        CF hx, hy, hz;
+        tile_pairs<T, MODE>(32, tiles + pb, jn, pe - pb, lane, st, ax, ay, az, dneg, dall, hx,
+                            hy, hz);
+        if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+            group_two_sum<32>(hx);
+            group_two_sum<32>(hy);
+            group_two_sum<32>(hz);
+            if constexpr (MODE == EXT_MIXED)
+                dall = group_sum<float, 32>(dall);
+        } else {
+            ax = group_sum<T, 32>(ax);
+            ay = group_sum<T, 32>(ay);
+            az = group_sum<T, 32>(az);
+        }
+        dneg = group_min<T, 32>(dneg);
+        if (lane == 0) {
+            T *o = slots[par][warp];
+            if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+                o[0] = hx.h;
+                o[1] = hx.l;
+                o[2] = hy.h;
+                o[3] = hy.l;
+                o[4] = hz.h;
+                o[5] = hz.l;
+            } else {
+                o[0] = ax;
+                o[1] = ay;
+                o[2] = az;
+            }
+            o[6] = dneg;
+            o[7] = (T)dall;
+        }
+        if (t == 0 && use_row)
+            grp_live[par][g] = live_seen;
+        gsync();
+
+        if constexpr (kAllStep) {
+            // ---- every warp combines the group's sums and steps ------------
+            double Edx = 0, Edy = 0, Edz = 0;
+            combine(par, ax, ay, az, dneg, dall, hx, hy, hz, Edx, Edy, Edz);
+            const bool hand_off = use_row && grp_live[par][g] <= (unsigned long long)P.tail_lines;
+            evals += (t == 0);
+            const int cls = ext_vertex<T, MODE>(P, line, s, lim, st, t, ax, ay, az, Edx, Edy,
+                                                Edz, dneg, r0x, r0y, r0z);
+            if (cls >= 0) {
+                if (t == 0)
+                    finish(cls);
+                gsync();
+                take();
+            } else if (hand_off) {
+                if (t == 0)
+                    save();
+                live = false;
+            }
+        } else {
+            // ---- the group's first warp combines and steps, then publishes
+            int flag = 0; // 1: the line goes on, 2: re-evaluate, 4: next line taken
+            double Edx = 0, Edy = 0, Edz = 0;
+            if (wg == 0) {
+                combine(par, ax, ay, az, dneg, dall, hx, hy, hz, Edx, Edy, Edz);
+                bool redo = false;
+                if constexpr (MODE == EXT_MIXED)
+                    redo = ext_ill_conditioned(P, dall, ax, ay, az);
+                flag = redo ? 2 : step(par, use_row, ax, ay, az, Edx, Edy, Edz, dneg);
+                if (lane == 0) {
+                    grp_flag[g] = flag;
+                    grp_pos[g][0] = st.px;
+                    grp_pos[g][1] = st.py;
+                    grp_pos[g][2] = st.pz;
+                }
+            }
+            gsync();
+            flag = grp_flag[g];
+            if constexpr (MODE == EXT_MIXED) {
+                if (flag == 2) {
+                    // an ill-conditioned sum: the group re-evaluates the field
+                    // in double-float (or FP64), each warp its W-th of the
+                    // resident records
+                    double fx = 0, fy = 0, fz = 0;
+                    if (!P.refine_fp64)
+                        field_df64<32>(recs + pb, pe - pb, lane, (float)st.px, (float)st.py,
+                                       (float)st.pz, fx, fy, fz);
+                    else
+                        field_fp64<32>(recs + pb, pe - pb, lane, (double)(float)st.px,
+                                       (double)(float)st.py, (double)(float)st.pz, fx, fy, fz);
+                    fx = group_sum<double, 32>(fx);
+                    fy = group_sum<double, 32>(fy);
+                    fz = group_sum<double, 32>(fz);
+                    if (lane == 0) {
+                        rslots[warp][0] = fx;
+                        rslots[warp][1] = fy;
+                        rslots[warp][2] = fz;
+                    }
+                    gsync();
+                    if (wg == 0) {
+                        const bool mine = lane < W;
+                        const double *rs = rslots[g * W + (mine ? lane : 0)];
+                        fx = group_sum<double, 32>(mine ? rs[0] : 0.0);
+                        fy = group_sum<double, 32>(mine ? rs[1] : 0.0);
+                        fz = group_sum<double, 32>(mine ? rs[2] : 0.0);
+                        ax = (T)(fx * kElectroK);
+                        ay = (T)(fy * kElectroK);
+                        az = (T)(fz * kElectroK);
+                        refines += (t == 0);
+                        flag = step(par, use_row, ax, ay, az, Edx, Edy, Edz, dneg);
+                        if (lane == 0) {
+                            grp_flag[g] = flag;
+                            grp_pos[g][0] = st.px;
+                            grp_pos[g][1] = st.py;
+                            grp_pos[g][2] = st.pz;
+                        }
+                    }
+                    gsync();
+                    flag = grp_flag[g];
+                }
+            }
+            if (flag & 4) {
+                take();
+            } else if (flag & 1) {
+                if (wg != 0) {
+                    st.px = grp_pos[g][0];
+                    st.py = grp_pos[g][1];
+                    st.pz = grp_pos[g][2];
+                }
+            } else {
+                live = false;
+            }
+        }
+    }
+    // counters: one atomic per warp
+    for (int o = 16; o; o >>= 1) {
+        evals += __shfl_xor_sync(0xffffffffu, evals, o);
+        refines += __shfl_xor_sync(0xffffffffu, refines, o);
+    }
+    if (lane == 0) {
+        if (evals)
+            atomicAdd(P.evals, evals);
+        if (refines)
+            atomicAdd(P.refines, refines);
+    }
+}
+
 template <class T, int MODE>
 cudaError_t launch_ext_wide_mode(const ExtParams<T> &p, const LaunchCfg &cfg,
                                  cudaStream_t stream)
 {
-    auto kern = ext_wide_kernel<T, MODE>;
+    auto kern = cfg.resident ? ext_wide_res_kernel<T, MODE> : ext_wide_kernel<T, MODE>;
     cudaError_t e =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (e != cudaSuccess)
