@@ -557,13 +557,14 @@ __global__ void __launch_bounds__(ext_cta_threads(MODE), 1)
 }
 
 // ---------------------------------------------------------------------------
-// The handed-off lines, W = P.wide warps per line (a group); the groups of a
-// CTA step in lockstep, three CTA barriers per row.  Warp w of a group sums
-// the charges of its W-th of each tile (or of the resident set) with all 32
-// lanes; the warps' sums meet in shared memory, the group's first warp (its
-// lead) combines them, runs the vertex step and publishes the new vertex,
-// which the other warps read after the row's last barrier.  A group whose
-// line ends takes the next handed-off line.
+// The handed-off lines with streamed charges, W = P.wide warps per line (a
+// group); the groups of a CTA share the tile ring, so they step in
+// lockstep, three CTA barriers per row.  Warp w of a group sums the charges
+// of its W-th of each tile with all 32 lanes; the warps' sums meet in shared
+// memory, the group's first warp (its lead) combines them, runs the vertex
+// step and publishes the new vertex, which the other warps read after the
+// row's last barrier.  A group whose line ends takes the next handed-off
+// line.  (Resident charges: ext_wide_res_kernel.)
 template <class T, int MODE>
 __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtParams<T> P)
 {
@@ -579,11 +580,10 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
-    const bool streamed = !P.resident;
-    const int ncw = streamed ? nwarps - 1 : nwarps;
-    const int NST = streamed ? P.stages : 1;
+    const int ncw = nwarps - 1;
+    const int NST = P.stages;
     const int W = P.wide;
-    if (NST > 8 || ncw < 1 || ncw > 32 || W < 1 || ncw % W != 0) {
+    if (P.resident || NST > 8 || ncw < 1 || ncw > 32 || W < 1 || ncw % W != 0) {
         if (threadIdx.x == 0)
             atomicCAS(P.err, 0, EM_DEVERR_CONFIG);
         return;
@@ -602,21 +602,7 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
     const ExtCont<T> *cont = static_cast<const ExtCont<T> *>(P.cont_in);
     __shared__ unsigned long long sh_live;
 
-    if (!streamed) {
-        if (threadIdx.x == 0) {
-            const uint32_t bytes = (uint32_t)P.p_pad * (uint32_t)sizeof(Rec);
-            mbar_arrive_expect_tx(full0, bytes);
-            const char *src = static_cast<const char *>(P.charges);
-            const uint32_t dst = smem_addr(tiles);
-            constexpr uint32_t CH = 32768;
-            for (uint32_t off = 0; off < bytes; off += CH)
-                bulk_g2s(dst + off, src + off, bytes - off < CH ? bytes - off : CH, full0);
-        }
-        // every thread passes the CTA barriers below, so none may leave here
-        mbar_wait(full0, 0, P.err);
-    }
-
-    if (streamed && warp == nwarps - 1) {
+    if (warp == nwarps - 1) {
         // ---- producer: the tiles of every row while any group has a line;
         // it passes the consumers' CTA barriers in the same order
         __syncthreads(); // first lines taken
@@ -708,9 +694,9 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
     __syncthreads(); // first lines taken
     take();
 
-    // this warp's W-th of the resident set (and of the re-evaluation's
-    // records), of a full wide tile and of the last, shorter one: fixed for
-    // the whole launch, so no division per row or tile
+    // this warp's W-th of the staged records (the re-evaluation's share), of
+    // a full wide tile and of the last, shorter one: fixed for the whole
+    // launch, so no division per row or tile
     const int pb = (int)((long long)P.p_pad * wg / W);
     const int pe = (int)((long long)P.p_pad * (wg + 1) / W);
     const int last_recs = P.p_pad - (P.n_tiles - 1) * P.tile_recs;
@@ -721,12 +707,12 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
 
     uint32_t it = 0;
     bool failed = false;
-    bool in_ring = true; // streamed: still consuming the tile ring
+    bool in_ring = true; // still consuming the tile ring
     unsigned row_iter = 0;
     for (;;) {
         if (!__syncthreads_or(live))
             break;
-        if (streamed && in_ring && !live) {
+        if (in_ring && !live) {
             // a group without a line now has none to come: its warps leave
             // the tile ring (all tiles of earlier rows are consumed)
             if (lane == 0)
@@ -749,29 +735,22 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
         T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
         float dall = 0.0f; // mixed: sum of q^2/r^4 over the pairs
         CF hx, hy, hz;
-        if (!streamed) {
-            const int jn = min(max(jneg_all - pb, 0), pe - pb);
-            if (live)
-                tile_pairs<T, MODE>(32, tiles + pb, jn, pe - pb, lane, st, ax, ay, az, dneg,
-                                    dall, hx, hy, hz);
-        } else {
-            for (int tile = 0; in_ring && tile < P.n_tiles; ++tile, ++it) {
-                const uint32_t sg = it % NST, ph = (it / NST) & 1;
-                if (!failed && !mbar_wait(full0 + 8 * sg, ph, P.err))
-                    failed = true;
-                if (!failed) {
-                    const int base = tile * P.tile_recs;
-                    const bool last_tile = tile == P.n_tiles - 1;
-                    const int b = last_tile ? lb : tb_, e = last_tile ? le : te;
-                    const int jt = min(max(jneg_all - base, 0), P.tile_recs);
-                    const int jn = min(max(jt - b, 0), e - b);
-                    if (live)
-                        tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane, st,
-                                            ax, ay, az, dneg, dall, hx, hy, hz);
-                    __syncwarp();
-                    if (lane == 0)
-                        mbar_arrive(empty0 + 8 * sg);
-                }
+        for (int tile = 0; in_ring && tile < P.n_tiles; ++tile, ++it) {
+            const uint32_t sg = it % NST, ph = (it / NST) & 1;
+            if (!failed && !mbar_wait(full0 + 8 * sg, ph, P.err))
+                failed = true;
+            if (!failed) {
+                const int base = tile * P.tile_recs;
+                const bool last_tile = tile == P.n_tiles - 1;
+                const int b = last_tile ? lb : tb_, e = last_tile ? le : te;
+                const int jt = min(max(jneg_all - base, 0), P.tile_recs);
+                const int jn = min(max(jt - b, 0), e - b);
+                if (live)
+                    tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane, st,
+                                        ax, ay, az, dneg, dall, hx, hy, hz);
+                __syncwarp();
+                if (lane == 0)
+                    mbar_arrive(empty0 + 8 * sg);
             }
         }
         // ---- each warp's sums into the slots -------------------------------
