@@ -277,3 +277,56 @@ def test_mixed_refinement_in_df64_equals_fp64(em, gpu, ext_case):
     rel = np.linalg.norm(fa - fb, axis=1) / np.linalg.norm(fa, axis=1)
     assert same >= 0.999, same
     assert rel.max() <= 1.2e-7, rel.max()
+
+
+@pytest.fixture(scope="module")
+def tail_case(em, orc):
+    """1023 lines of the 4096-charge workload (every 32nd seed): few enough
+    that the lane-group kernel hands them all to the resident-charge tail
+    kernel, in rounds of 2, 4, 8 and 16 warps per line."""
+    ch, seeds, _ = em.workloads.make("gpu_4096", seed=1234)
+    seeds = seeds[::32].astype(np.float32)
+    steps = 600
+    ref = orc.trace_lines_f64(ch.astype(np.float64), seeds.astype(np.float64),
+                              steps, 1.0, 0.5)
+    return ch, seeds, steps, ref
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed", "df64"])
+def test_resident_tail_matches_fp64_oracle(em, gpu, tail_case, precision):
+    """Resident charges, lines handed to the tail kernel (one group barrier
+    per row; the FP32 step repeated in every warp of a group, the other
+    modes' steps on its first warp): classes and vertices meet the oracle
+    criteria, and every evaluated vertex is counted once."""
+    ch, seeds, steps, ref = tail_case
+    lib = em.load()
+    before = lib.em_launch_count()
+    out = em.trace_lines(seeds, ch, steps, 1.0, 0.5, precision=precision)
+    launches = lib.em_launch_count() - before
+    assert launches >= 3, launches  # staging, lane groups, tail rounds
+    agree, vok, gl, gc = compare(out, ref)
+    assert agree >= CLASS_AGREE, agree
+    assert vok >= CLASS_AGREE, vok
+    assert np.all((gl >= 1) & (gl <= steps))
+    assert out["perf"].pairs == pytest.approx(
+        float(np.sum(gl - 1 + (gc != 0))) * len(ch), rel=0, abs=0)
+
+
+def test_resident_tail_equals_lane_groups(em, gpu, tail_case):
+    """The tail kernel changes only the summation order: lengths and classes
+    equal the deterministic run's (lane groups only) and vertices agree
+    within tolerance over the first 200 rows."""
+    ch, seeds, steps, _ = tail_case
+    a = em.trace_lines(seeds, ch, steps, 1.0, 0.5, deterministic=True)
+    b = em.trace_lines(seeds, ch, steps, 1.0, 0.5)
+    same = (a["len"] == b["len"]) & (a["cls"] == b["cls"])
+    assert same.mean() >= CLASS_AGREE, same.mean()
+    with np.errstate(invalid="ignore", over="ignore"):
+        A = a["vertices"].astype(np.float64)
+        B = b["vertices"].astype(np.float64)
+    ok = 0
+    for i in range(len(seeds)):
+        m = min(a["len"][i], b["len"][i], 200)
+        err = np.abs(A[:, :m, i] - B[:, :m, i]) / np.maximum(np.abs(A[:, :m, i]), 1)
+        ok += err.max() <= VERTEX_RTOL
+    assert ok / len(seeds) >= CLASS_AGREE, ok / len(seeds)
