@@ -207,6 +207,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
         e = cudaMemcpyAsync(c.charges_raw, charges, p * rec, kin, s);
     if (e == cudaSuccess)
         e = launch_ext_stage<T>(c.charges_raw, (int)p, c.charges, p_pad, gran,
+                                mode == EXT_MIXED ? tile : 0,
                                 reinterpret_cast<int *>(status + kOffMeta),
                                 reinterpret_cast<float *>(status + kOffQabs), s);
     if (e == cudaSuccess && !o.device_ptrs) {
@@ -250,6 +251,7 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
     prm.p_pad = p_pad;
     prm.n_tiles = n_tiles;
     prm.tile_recs = tile;
+    prm.stage_recs = tile;
     prm.stages = cfg.stages;
     prm.resident = cfg.resident;
     prm.regroup = o.deterministic ? 0 : 1;

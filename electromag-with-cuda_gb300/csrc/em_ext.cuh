@@ -11,11 +11,6 @@
 namespace em {
 namespace {
 
-// pairs per lane between compensated additions: 16 keeps the FP32 chunk
-// sums' error within the mixed mode's conditioning test (64 left 0.09 % of
-// the GPU-scale set's vertices at 1.1-1.6e-6)
-constexpr int kChunk = 16;
-
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 {
     s = __fadd_rn(a, b);
@@ -93,56 +88,106 @@ __device__ __forceinline__ void pairs_fast(const ChargeD *tile, int jneg, int co
     }
 }
 
-// Mixed: FP32 pairs with the inv^3 correction over records [lo, hi) (lo a
-// multiple of TPL), compensated every kChunk pairs; l2 gets the sum of the
-// terms' squared sizes q^2/r^4 (the conditioning test's measure) and, for
-// NEG (the negative block), dmin the nearest distance^2 of the range.
+// Mixed arithmetic: FP32 records in the paired layout (blocks of `block`
+// records, each block's A plane {xa, xb, ya, yb} of block/2 float4, then its
+// B plane {za, zb, qa, qb}), two charges per packed .f32x2 instruction.
+//
+// Term.  With y = rsqrt(r2) (relative error d) and w = y*y, the product
+// r2*w = 1 + 2d, and q/|r|^3 = q y^3 (2.5 - 1.5 r2 w) + O(d^2): one Newton
+// correction.  Written as v * (r2 w - 5/3) with v = q y w it costs two
+// operations beyond the plain term and yields -(2/3) q/|r|^3; the factor
+// -3/2 (and the rounding of 5/3 to FP32, a constant factor) goes into the
+// per-vertex scale kMixScale.
+constexpr float kMixC53 = -1.66666663f; // -5/3 rounded to FP32
+// -(3/2) / ((1 + kMixC53) / (1 - 5/3)): the terms' scale back to q r/|r|^3
+constexpr double kMixScale = -1.5 / ((1.0 + (double)kMixC53) / (1.0 - 5.0 / 3.0));
+// charge pairs per lane and compensated chunk of the extended tracer (16
+// terms: 64 left 0.09 % of the 4096-charge set's vertices at 1.1-1.6e-6)
+constexpr int kMixChunkPairs = 8;
+
+// Charge pairs [lo, hi) of one paired block (planes A, B) for lane t of
+// TPL: FP32 chunk sums of kMixChunkPairs pairs (both halves folded) into the
+// compensated sums; L2 collects sum_j q_j^2 y_j^4 (the conditioning test's
+// measure, from q y and v); for NEG (the negative block) dmin the nearest
+// distance^2.
 template <int TPL, bool NEG>
-__device__ __forceinline__ void mixed_range(const float4 *tile, int lo, int hi, int t, float px,
-                                            float py, float pz, CF &hx, CF &hy, CF &hz,
-                                            float &dmin, float &l2)
+__device__ __forceinline__ void mixed_pk_range(const ulonglong2 *A, const ulonglong2 *B, int lo,
+                                               int hi, int t, u64 PX, u64 PY, u64 PZ, CF &hx,
+                                               CF &hy, CF &hz, float &dmin, u64 &L2)
 {
-    for (int j0 = lo + t; j0 < hi; j0 += TPL * kChunk) {
-        const int j1 = min(hi, j0 + TPL * kChunk);
-        float ax = 0, ay = 0, az = 0;
-#pragma unroll 4
-        for (int j = j0; j < j1; j += TPL) {
-            const float4 c = tile[j];
-            const float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (NEG)
-                dmin = fminf(dmin, r2);
-            const float inv = rsqrt_fast(r2);
-            const float inv2 = inv * inv;
-            const float qi = c.w * inv;
-            const float s0 = qi * inv2;
-            // inv^3 carries three times the relative error eps of inv; to
-            // first order r2 inv2 - 1 = 2 eps, so s0 (2.5 - 1.5 r2 inv2) =
-            // s0 / (1 + 3 eps): one Newton correction, three FMA-pipe ops
-            const float g = fmaf(-1.5f * r2, inv2, 2.5f);
-            const float sc = s0 * g;
-            l2 = fmaf(qi, s0, l2);
-            ax = fmaf(sc, dx, ax);
-            ay = fmaf(sc, dy, ay);
-            az = fmaf(sc, dz, az);
+    const u64 C53 = f2_pack(kMixC53, kMixC53);
+    u64 AX, AY, AZ;
+    auto term = [&](int jp) {
+        const ulonglong2 a = A[jp], b = B[jp];
+        const u64 dx = f2_sub(PX, a.x), dy = f2_sub(PY, a.y), dz = f2_sub(PZ, b.x);
+        const u64 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+        if (NEG) {
+            float ra, rb;
+            f2_unpack(r2, ra, rb);
+            dmin = fminf(dmin, fminf(ra, rb));
         }
-        hx.add(ax);
-        hy.add(ay);
-        hz.add(az);
+        const u64 y = f2_rsqrt(r2);
+        const u64 w = f2_mul(y, y);
+        const u64 qy = f2_mul(b.y, y);
+        const u64 v = f2_mul(qy, w);
+        const u64 sc = f2_mul(v, f2_fma(r2, w, C53));
+        AX = f2_fma(sc, dx, AX);
+        AY = f2_fma(sc, dy, AY);
+        AZ = f2_fma(sc, dz, AZ);
+        L2 = f2_fma(qy, v, L2);
+    };
+    for (int j0 = lo + t; j0 < hi; j0 += TPL * kMixChunkPairs) {
+        AX = AY = AZ = 0ull;
+        if (j0 + TPL * (kMixChunkPairs - 1) < hi) {
+            // a full chunk: a fixed trip count, unrolled
+#pragma unroll
+            for (int u = 0; u < kMixChunkPairs; ++u)
+                term(j0 + u * TPL);
+        } else {
+            // a short range (the tail kernels' rows): unrolled as well, so
+            // its pairs overlap instead of forming one latency chain
+#pragma unroll 4
+            for (int jp = j0; jp < hi; jp += TPL)
+                term(jp);
+        }
+        float u, v;
+        f2_unpack(AX, u, v);
+        hx.add(u + v);
+        f2_unpack(AY, u, v);
+        hy.add(u + v);
+        f2_unpack(AZ, u, v);
+        hz.add(u + v);
     }
 }
 
-// Mixed pairs over a tile: [0, jneg) are negative charges (nearest one
-// tracked); l2 sums q^2/r^4 over every pair.
+// Mixed pairs [lo, hi) of one paired block whose first jn2 pairs are
+// negative charges (nearest one tracked); l2 gets sum_j q_j^2 / r_j^4.  The
+// sums are in the terms' scaled units (times kMixScale: q r/|r|^3).
+template <int TPL>
+__device__ __forceinline__ void mixed_pk(const ulonglong2 *A, const ulonglong2 *B, int jn2,
+                                         int lo, int hi, int t, float px, float py, float pz,
+                                         CF &hx, CF &hy, CF &hz, float &dneg, float &l2)
+{
+    const u64 PX = f2_pack(px, px), PY = f2_pack(py, py), PZ = f2_pack(pz, pz);
+    u64 L2 = 0ull;
+    float dn = 3.0e38f, unused = 0;
+    mixed_pk_range<TPL, true>(A, B, lo, min(hi, jn2), t, PX, PY, PZ, hx, hy, hz, dn, L2);
+    mixed_pk_range<TPL, false>(A, B, max(lo, jn2), hi, t, PX, PY, PZ, hx, hy, hz, unused, L2);
+    float u, v;
+    f2_unpack(L2, u, v);
+    l2 += u + v;
+    dneg = fminf(dneg, dn);
+}
+
+// Mixed pairs over one staged tile: `tile` is a paired block of `count`
+// records whose first jneg are negative charges.
 template <int TPL>
 __device__ __forceinline__ void pairs_mixed(const float4 *tile, int jneg, int count, int t,
                                             float px, float py, float pz, CF &hx, CF &hy, CF &hz,
                                             float &dneg, float &l2)
 {
-    float dn = 3.0e38f, unused = 0;
-    mixed_range<TPL, true>(tile, 0, jneg, t, px, py, pz, hx, hy, hz, dn, l2);
-    mixed_range<TPL, false>(tile, jneg, count, t, px, py, pz, hx, hy, hz, unused, l2);
-    dneg = fminf(dneg, dn);
+    const ulonglong2 *A = reinterpret_cast<const ulonglong2 *>(tile);
+    mixed_pk<TPL>(A, A + count / 2, jneg / 2, 0, count / 2, t, px, py, pz, hx, hy, hz, dneg, l2);
 }
 
 // FP64 field at (px, py, pz) from the staged records in global memory, lane
@@ -310,6 +355,62 @@ __device__ __forceinline__ void field_df64(const float4 *charges, int count, int
     ax += (double)hx.h + (double)hx.l;
     ay += (double)hy.h + (double)hy.l;
     az += (double)hz.h + (double)hz.l;
+}
+
+// Double-float (F64: FP64) field at an FP32 point from paired-layout
+// records (blocks of `block` records, as staged for the mixed mode), charge
+// pairs [lo, hi) of the whole staged set, lane t of TPL taking pairs
+// lo + t, lo + t + TPL, ...; the lane's partial sums in FP64 (summed later
+// across the group).
+template <int TPL, bool F64>
+__device__ __forceinline__ void field_pk(const float4 *rec, int block, int lo, int hi, int t,
+                                         float px, float py, float pz, double &ax, double &ay,
+                                         double &az)
+{
+    const int half = block / 2;
+    int gp = lo + t;
+    int b = gp / half, jp = gp - b * half;
+    CF hx, hy, hz;
+    double sx = 0, sy = 0, sz = 0;
+    auto term = [&](const float4 &c) {
+        if constexpr (F64) {
+            const double dx = (double)px - (double)c.x, dy = (double)py - (double)c.y,
+                         dz = (double)pz - (double)c.z;
+            const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+            const double inv = 1.0 / sqrt(r2);
+            const double s = (double)c.w * inv * inv * inv;
+            sx = fma(s, dx, sx);
+            sy = fma(s, dy, sy);
+            sz = fma(s, dz, sz);
+        } else {
+            DF tx, ty, tz;
+            float r2h;
+            df_pair(px, py, pz, c, tx, ty, tz, r2h);
+            cf_add_df(hx, tx);
+            cf_add_df(hy, ty);
+            cf_add_df(hz, tz);
+        }
+    };
+    for (; gp < hi; gp += TPL) {
+        const float4 A = rec[(size_t)b * block + jp];
+        const float4 B = rec[(size_t)b * block + half + jp];
+        term(make_float4(A.x, A.z, B.x, B.z));
+        term(make_float4(A.y, A.w, B.y, B.w));
+        jp += TPL;
+        while (jp >= half) {
+            jp -= half;
+            ++b;
+        }
+    }
+    if constexpr (F64) {
+        ax += sx;
+        ay += sy;
+        az += sz;
+    } else {
+        ax += (double)hx.h + (double)hx.l;
+        ay += (double)hy.h + (double)hy.l;
+        az += (double)hz.h + (double)hz.l;
+    }
 }
 
 template <class T, int TPL>

@@ -107,6 +107,7 @@ template <class T> struct ExtParams {
     int *len, *cls;
     unsigned long long *next_line, *evals, *refines;
     int p_pad, n_tiles, tile_recs, stages, resident;
+    int stage_recs;                 // staged tile (the mixed mode's paired blocks)
     int regroup;                    // widen lane groups once the queue is dry
     int refine_fp64;                // mixed: re-evaluate in FP64 (else double-float)
     double kappa2;                  // mixed: the conditioning test's kappa^2
@@ -137,7 +138,7 @@ template <class T> struct ExtCont {
 
 template <class T>
 cudaError_t launch_ext_stage(const void *raw, int p, void *staged, int p_pad, int gran,
-                             int *meta, float *qabs, cudaStream_t stream);
+                             int block, int *meta, float *qabs, cudaStream_t stream);
 template <class T>
 cudaError_t launch_ext_trace(const ExtParams<T> &p, const struct LaunchCfg &cfg, int mode,
                              cudaStream_t stream);

@@ -43,11 +43,35 @@ namespace {
 // ---------------------------------------------------------------------------
 // Staging: stable partition of p raw records into
 //   [negatives | pad to gran][positives | pad to p_pad], one CTA of 1024.
+// block > 0 (the mixed mode): in the paired layout, blocks of `block`
+// records, each the block's A plane {xa, xb, ya, yb} then its B plane
+// {za, zb, qa, qb} (record pairs 2i, 2i + 1 of the block).
 // meta[0] = size of the padded negative block (records).
 // qabs[0] = largest |q| (float).
 template <class T>
+__device__ __forceinline__ void stage_put(T *staged, int block, int r, T x, T y, T z, T q)
+{
+    if (block == 0) {
+        T *d = staged + 4 * (size_t)r;
+        d[0] = x;
+        d[1] = y;
+        d[2] = z;
+        d[3] = q;
+        return;
+    }
+    const int b = r / block, i = r - b * block, jp = i >> 1, h = i & 1;
+    T *A = staged + 4 * ((size_t)b * block + jp);
+    T *B = staged + 4 * ((size_t)b * block + block / 2 + jp);
+    A[h] = x;
+    A[2 + h] = y;
+    B[h] = z;
+    B[2 + h] = q;
+}
+
+template <class T>
 __global__ void __launch_bounds__(1024)
-    ext_stage_kernel(const T *raw, int p, T *staged, int p_pad, int gran, int *meta, float *qabs)
+    ext_stage_kernel(const T *raw, int p, T *staged, int p_pad, int gran, int block, int *meta,
+                     float *qabs)
 {
     __shared__ int scan[1024];
     __shared__ float qm[32];
@@ -77,20 +101,13 @@ __global__ void __launch_bounds__(1024)
         wp = neg_pad;
     for (int i = b; i < e; ++i) {
         const T *r = raw + 4 * (size_t)i;
-        T *d = staged + 4 * (size_t)(r[3] < T(0) ? wn++ : wp++);
-        d[0] = r[0];
-        d[1] = r[1];
-        d[2] = r[2];
-        d[3] = r[3];
+        stage_put(staged, block, r[3] < T(0) ? wn++ : wp++, r[0], r[1], r[2], r[3]);
     }
     // pad records {1e15, 1e15, 1e15, 0}: exactly zero contribution
     const int pos_end = neg_pad + (p - total_neg);
     for (int i = tid; i < p_pad; i += 1024) {
-        if ((i >= total_neg && i < neg_pad) || i >= pos_end) {
-            T *d = staged + 4 * (size_t)i;
-            d[0] = d[1] = d[2] = T(1e15);
-            d[3] = T(0);
-        }
+        if ((i >= total_neg && i < neg_pad) || i >= pos_end)
+            stage_put(staged, block, i, T(1e15), T(1e15), T(1e15), T(0));
     }
     for (int o = 16; o; o >>= 1)
         qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, o));
@@ -112,11 +129,22 @@ template <class T, int MODE>
 __device__ __forceinline__ void ext_field(T &ax, T &ay, T &az, const CF &hx, const CF &hy,
                                           const CF &hz, double &Edx, double &Edy, double &Edz)
 {
+    Edx = Edy = Edz = 0;
+    if constexpr (MODE == EXT_MIXED) {
+        // the sums are in the packed terms' scaled units: times kMixScale
+        // and the Coulomb constant, a double-float pair, rounded once
+        constexpr double kScale = kMixScale * kElectroK;
+        constexpr float kScaleH = (float)kScale;
+        constexpr float kScaleL = (float)(kScale - (double)kScaleH);
+        ax = fmaf(hx.h, kScaleH, fmaf(hx.h, kScaleL, hx.l * kScaleH));
+        ay = fmaf(hy.h, kScaleH, fmaf(hy.h, kScaleL, hy.l * kScaleH));
+        az = fmaf(hz.h, kScaleH, fmaf(hz.h, kScaleL, hz.l * kScaleH));
+        return;
+    }
     const T K = (T)kElectroK;
     ax = mul_rn(ax, K);
     ay = mul_rn(ay, K);
     az = mul_rn(az, K);
-    Edx = Edy = Edz = 0;
     if constexpr (MODE == EXT_DF64) {
         Edx = ((double)hx.h + (double)hx.l) * kElectroK;
         Edy = ((double)hy.h + (double)hy.l) * kElectroK;
@@ -480,10 +508,11 @@ __global__ void __launch_bounds__(ext_cta_threads(MODE), 1)
                 const float rz = __shfl_sync(0xffffffffu, (float)st.pz, src);
                 double fx = 0, fy = 0, fz = 0;
                 if (!P.refine_fp64)
-                    field_df64<32>(rec, P.p_pad, lane, rx, ry, rz, fx, fy, fz);
+                    field_pk<32, false>(rec, P.stage_recs, 0, P.p_pad / 2, lane, rx, ry, rz, fx,
+                                        fy, fz);
                 else
-                    field_fp64<32>(rec, P.p_pad, lane, (double)rx, (double)ry, (double)rz, fx,
-                                   fy, fz);
+                    field_pk<32, true>(rec, P.stage_recs, 0, P.p_pad / 2, lane, rx, ry, rz, fx,
+                                       fy, fz);
                 fx = group_sum<double, 32>(fx);
                 fy = group_sum<double, 32>(fy);
                 fz = group_sum<double, 32>(fz);
@@ -704,6 +733,10 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
     const int te = (int)((long long)P.tile_recs * (wg + 1) / W);
     const int lb = (int)((long long)last_recs * wg / W);
     const int le = (int)((long long)last_recs * (wg + 1) / W);
+    // mixed: the warp's W-th of all staged charge pairs (the
+    // re-evaluation's share)
+    const int rb = (int)((long long)(P.p_pad / 2) * wg / W);
+    const int re = (int)((long long)(P.p_pad / 2) * (wg + 1) / W);
 
     uint32_t it = 0;
     bool failed = false;
@@ -743,11 +776,28 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
                 const int base = tile * P.tile_recs;
                 const bool last_tile = tile == P.n_tiles - 1;
                 const int b = last_tile ? lb : tb_, e = last_tile ? le : te;
-                const int jt = min(max(jneg_all - base, 0), P.tile_recs);
-                const int jn = min(max(jt - b, 0), e - b);
-                if (live)
-                    tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane, st,
-                                        ax, ay, az, dneg, dall, hx, hy, hz);
+                if constexpr (MODE == EXT_MIXED) {
+                    // paired blocks of the staged tile size: the warp's
+                    // W-th of the wide tile's charge pairs [b/2, e/2), block
+                    // by block
+                    const int SR = P.stage_recs, half = SR / 2;
+                    const ulonglong2 *blk =
+                        reinterpret_cast<const ulonglong2 *>(tiles + sg * P.tile_recs);
+                    for (int k = (b / 2) / half; live && k * half < e / 2; ++k) {
+                        const int lo = max(b / 2 - k * half, 0);
+                        const int hi = min(e / 2 - k * half, half);
+                        const int jk = min(max(jneg_all - (base + k * SR), 0), SR);
+                        const ulonglong2 *Ak = blk + (size_t)k * SR;
+                        mixed_pk<32>(Ak, Ak + half, jk / 2, lo, hi, lane, st.px, st.py, st.pz,
+                                     hx, hy, hz, dneg, dall);
+                    }
+                } else {
+                    const int jt = min(max(jneg_all - base, 0), P.tile_recs);
+                    const int jn = min(max(jt - b, 0), e - b);
+                    if (live)
+                        tile_pairs<T, MODE>(32, tiles + sg * P.tile_recs + b, jn, e - b, lane,
+                                            st, ax, ay, az, dneg, dall, hx, hy, hz);
+                }
                 __syncwarp();
                 if (lane == 0)
                     mbar_arrive(empty0 + 8 * sg);
@@ -830,14 +880,13 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
                 const bool gredo = grp_flag[g] == 2;
                 double fx = 0, fy = 0, fz = 0;
                 if (gredo) {
-                    const int cb = pb, ce = pe;
-                    const float4 *cr = reinterpret_cast<const float4 *>(P.charges) + cb;
+                    const float4 *cr = reinterpret_cast<const float4 *>(P.charges);
                     if (!P.refine_fp64)
-                        field_df64<32>(cr, ce - cb, lane, (float)st.px, (float)st.py,
-                                       (float)st.pz, fx, fy, fz);
+                        field_pk<32, false>(cr, P.stage_recs, rb, re, lane, (float)st.px,
+                                            (float)st.py, (float)st.pz, fx, fy, fz);
                     else
-                        field_fp64<32>(cr, ce - cb, lane, (double)(float)st.px,
-                                       (double)(float)st.py, (double)(float)st.pz, fx, fy, fz);
+                        field_pk<32, true>(cr, P.stage_recs, rb, re, lane, (float)st.px,
+                                           (float)st.py, (float)st.pz, fx, fy, fz);
                     fx = group_sum<double, 32>(fx);
                     fy = group_sum<double, 32>(fy);
                     fz = group_sum<double, 32>(fz);
@@ -1032,6 +1081,9 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
     const int pb = (int)((long long)P.p_pad * wg / W);
     const int pe = (int)((long long)P.p_pad * (wg + 1) / W);
     const int jn = min(max(jneg_all - pb, 0), pe - pb);
+    // mixed (paired layout, one block): the warp's W-th of the charge pairs
+    const int rb = (int)((long long)(P.p_pad / 2) * wg / W);
+    const int re = (int)((long long)(P.p_pad / 2) * (wg + 1) / W);
     const float4 *recs = reinterpret_cast<const float4 *>(tiles);
 
     unsigned long long evals = 0, refines = 0, live_seen = ~0ull;
@@ -1122,8 +1174,14 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
         T ax = 0, ay = 0, az = 0, dneg = T(3.0e38);
         float dall = 0.0f; // mixed: sum of q^2/r^4 over the pairs
         CF hx, hy, hz;
-        tile_pairs<T, MODE>(32, tiles + pb, jn, pe - pb, lane, st, ax, ay, az, dneg, dall, hx,
-                            hy, hz);
+        if constexpr (MODE == EXT_MIXED) {
+            const ulonglong2 *A = reinterpret_cast<const ulonglong2 *>(tiles);
+            mixed_pk<32>(A, A + P.p_pad / 2, jneg_all / 2, rb, re, lane, st.px, st.py, st.pz, hx,
+                         hy, hz, dneg, dall);
+        } else {
+            tile_pairs<T, MODE>(32, tiles + pb, jn, pe - pb, lane, st, ax, ay, az, dneg, dall,
+                                hx, hy, hz);
+        }
         if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
             group_two_sum<32>(hx);
             group_two_sum<32>(hy);
@@ -1201,11 +1259,11 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
                     // resident records
                     double fx = 0, fy = 0, fz = 0;
                     if (!P.refine_fp64)
-                        field_df64<32>(recs + pb, pe - pb, lane, (float)st.px, (float)st.py,
-                                       (float)st.pz, fx, fy, fz);
+                        field_pk<32, false>(recs, P.p_pad, rb, re, lane, (float)st.px,
+                                            (float)st.py, (float)st.pz, fx, fy, fz);
                     else
-                        field_fp64<32>(recs + pb, pe - pb, lane, (double)(float)st.px,
-                                       (double)(float)st.py, (double)(float)st.pz, fx, fy, fz);
+                        field_pk<32, true>(recs, P.p_pad, rb, re, lane, (float)st.px,
+                                           (float)st.py, (float)st.pz, fx, fy, fz);
                     fx = group_sum<double, 32>(fx);
                     fy = group_sum<double, 32>(fy);
                     fz = group_sum<double, 32>(fz);
@@ -1308,11 +1366,13 @@ cudaError_t launch_ext_mode(const ExtParams<T> &p, const LaunchCfg &cfg, cudaStr
 
 template <class T>
 cudaError_t launch_ext_stage(const void *raw, int p, void *staged, int p_pad, int gran,
-                             int *meta, float *qabs, cudaStream_t stream)
+                             int block, int *meta, float *qabs, cudaStream_t stream)
 {
+    if (block < 0 || (block && (block & 1 || p_pad % block)))
+        return cudaErrorInvalidValue;
     ext_stage_kernel<T><<<1, 1024, 0, stream>>>(static_cast<const T *>(raw), p,
-                                                static_cast<T *>(staged), p_pad, gran, meta,
-                                                qabs);
+                                                static_cast<T *>(staged), p_pad, gran, block,
+                                                meta, qabs);
     count_launch(1);
     return cudaGetLastError();
 }
@@ -1355,9 +1415,9 @@ cudaError_t launch_ext_wide<double>(const ExtParams<double> &p, const LaunchCfg 
     return launch_ext_wide_mode<double, EXT_FAST>(p, cfg, stream);
 }
 
-template cudaError_t launch_ext_stage<float>(const void *, int, void *, int, int, int *, float *,
-                                             cudaStream_t);
-template cudaError_t launch_ext_stage<double>(const void *, int, void *, int, int, int *,
+template cudaError_t launch_ext_stage<float>(const void *, int, void *, int, int, int, int *,
+                                             float *, cudaStream_t);
+template cudaError_t launch_ext_stage<double>(const void *, int, void *, int, int, int, int *,
                                               float *, cudaStream_t);
 
 } // namespace em

@@ -173,10 +173,7 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
 // terms, not of their sum.  (Squared chunk sums would cost less but miss
 // terms that cancel inside a chunk, such as the two charges of a dipole
 // stored side by side.)
-constexpr int kMixChunk = 32;                       // charge pairs per lane and chunk
-constexpr float kMixC53 = -1.66666663f;             // -5/3 rounded to FP32
-// -(3/2) / ((1 + kMixC53) / (1 - 5/3)): the terms' scale back to q r/|r|^3
-constexpr double kMixScale = -1.5 / ((1.0 + (double)kMixC53) / (1.0 - 5.0 / 3.0));
+constexpr int kMixChunk = 32; // charge pairs per lane and chunk (kMixC53, kMixScale: em_ext.cuh)
 
 template <int TPL, int KL>
 __device__ __forceinline__ void accumulate_mixed(const float4 *tile, int count, int t,
