@@ -330,3 +330,30 @@ def test_resident_tail_equals_lane_groups(em, gpu, tail_case):
         err = np.abs(A[:, :m, i] - B[:, :m, i]) / np.maximum(np.abs(A[:, :m, i]), 1)
         ok += err.max() <= VERTEX_RTOL
     assert ok / len(seeds) >= CLASS_AGREE, ok / len(seeds)
+
+
+def test_resident_tail_step_limits(em, gpu, tail_case):
+    """Per-line step limits through the tail kernel: no line runs past its
+    limit, and a line ends by its limit exactly when it reaches it."""
+    ch, seeds, steps, _ = tail_case
+    rng = np.random.default_rng(11)
+    lim = rng.integers(1, steps + 1, len(seeds)).astype(np.int32)
+    lim[::7] = steps                        # some long lines for the tail
+    out = em.trace_lines(seeds, ch, steps, 1.0, 0.5, steps_per_line=lim)
+    gl, gc = out["len"], out["cls"]
+    assert np.all(gl <= np.maximum(lim, 1))
+    assert np.all((gc == 0) == (gl == np.maximum(lim, 1)))
+
+
+def test_resident_tail_mixed_field_within_1e6(em, gpu, orc, tail_case):
+    """Mixed mode through the tail kernels: the field stored at every
+    evaluated vertex is within 1e-6 of the FP64 field at that point (the
+    conditioning test and re-evaluations run there too)."""
+    ch, seeds, steps, _ = tail_case
+    out = em.trace_lines(seeds, ch, steps, 1.0, 0.5, precision="mixed",
+                         want_field=True)
+    pts, fld = _fields_at_vertices(out, 1)
+    e64 = orc.field_f64(pts, ch.astype(np.float64))
+    rel = np.linalg.norm(fld - e64, axis=1) / np.linalg.norm(e64, axis=1)
+    assert rel.max() <= 1e-6, (rel.max(), (rel > 1e-6).sum())
+    assert np.median(rel) <= 2e-7, np.median(rel)
