@@ -357,3 +357,38 @@ def test_resident_tail_mixed_field_within_1e6(em, gpu, orc, tail_case):
     rel = np.linalg.norm(fld - e64, axis=1) / np.linalg.norm(e64, axis=1)
     assert rel.max() <= 1e-6, (rel.max(), (rel > 1e-6).sum())
     assert np.median(rel) <= 2e-7, np.median(rel)
+
+
+@pytest.mark.parametrize("streamed", [False, True])
+@pytest.mark.parametrize("p,sign", [(0, 0), (1, 1), (1, -1), (3, 0), (5, 1), (63, 0),
+                                    (65, -1), (1001, 0)])
+def test_mixed_small_and_odd_sets(em, gpu, orc, p, sign, streamed):
+    """The mixed mode's paired layout with odd, tiny and one-signed charge
+    sets (pad records fill the last pair), resident and in 8-record streamed
+    tiles: classes and vertices against the FP64 oracle, and the stored
+    field within 1e-6 of FP64 wherever the field is not zero."""
+    rng = np.random.default_rng(100 * p + sign + 1)
+    ch = np.zeros((p, 4), np.float32)
+    ch[:, :3] = rng.uniform(-5, 5, (p, 3))
+    q = rng.uniform(1, 3, p)
+    q *= np.where(rng.random(p) < 0.5, -1.0, 1.0) if sign == 0 else sign
+    ch[:, 3] = q
+    seeds = rng.uniform(-6, 6, (256 if p > 100 else 64, 3)).astype(np.float32)
+    steps = 60
+    kw = dict(force_streamed=True, tile_charges=8) if streamed else {}
+    out = em.trace_lines(seeds, ch, steps, 1.0, 0.5, precision="mixed",
+                         want_field=True, **kw)
+    ref = orc.trace_lines_f64(ch.astype(np.float64), seeds.astype(np.float64),
+                              steps, 1.0, 0.5)
+    agree, vok, gl, gc = compare(out, ref)
+    assert agree >= 0.95, agree
+    assert vok >= 0.95, vok
+    if p == 0:
+        assert np.all(gc == 2) and np.all(gl == 1)  # no field: null at once
+        return
+    pts, fld = _fields_at_vertices(out, 1)
+    e64 = orc.field_f64(pts, ch.astype(np.float64))
+    n64 = np.linalg.norm(e64, axis=1)
+    ok = n64 > 0
+    rel = np.linalg.norm(fld - e64, axis=1)[ok] / n64[ok]
+    assert rel.max() <= 1e-6, (rel.max(), (rel > 1e-6).sum())
