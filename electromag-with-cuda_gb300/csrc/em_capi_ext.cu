@@ -148,9 +148,9 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             dez = dey + elems;
         }
     }
-    // tail hand-off (not in deterministic mode: the wide kernel sums a
+    // tail hand-off (not in deterministic mode: the tail kernels sum a
     // line's charges in another grouping): the lines left once at most half
-    // the warp slots would hold one each go to the wide kernel.  With
+    // the warp slots would hold one each go to the tail kernels.  With
     // streamed tiles every warp of a CTA waits on every tile, so a few long
     // lines on a few warps hold whole SMs; spread over many warps they use
     // them.  With resident charges a lone line gains from more warps as

@@ -190,25 +190,6 @@ __device__ __forceinline__ void pairs_mixed(const float4 *tile, int jneg, int co
     mixed_pk<TPL>(A, A + count / 2, jneg / 2, 0, count / 2, t, px, py, pz, hx, hy, hz, dneg, l2);
 }
 
-// FP64 field at (px, py, pz) from the staged records in global memory, lane
-// t of TPL (summed later across the group).
-template <int TPL>
-__device__ __forceinline__ void field_fp64(const float4 *charges, int count, int t, double px,
-                                           double py, double pz, double &ax, double &ay,
-                                           double &az)
-{
-    for (int j = t; j < count; j += TPL) {
-        const float4 c = charges[j];
-        const double dx = px - (double)c.x, dy = py - (double)c.y, dz = pz - (double)c.z;
-        const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-        const double inv = 1.0 / sqrt(r2);
-        const double s = (double)c.w * inv * inv * inv;
-        ax = fma(s, dx, ax);
-        ay = fma(s, dy, ay);
-        az = fma(s, dz, az);
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Double-float arithmetic (a value is h + l, two FP32 words, about 48 bits):
 // error-free sums and products by the classical transformations (Knuth's
@@ -334,27 +315,6 @@ __device__ __forceinline__ void pairs_df64(const float4 *tile, int jneg, int cou
         cf_add_df(hy, ty);
         cf_add_df(hz, tz);
     }
-}
-
-// Double-float field at an FP32 point from the staged records in global
-// memory, lane t of TPL (summed later across the group), returned in FP64.
-template <int TPL>
-__device__ __forceinline__ void field_df64(const float4 *charges, int count, int t, float px,
-                                           float py, float pz, double &ax, double &ay,
-                                           double &az)
-{
-    CF hx, hy, hz;
-    for (int j = t; j < count; j += TPL) {
-        DF tx, ty, tz;
-        float r2h;
-        df_pair(px, py, pz, charges[j], tx, ty, tz, r2h);
-        cf_add_df(hx, tx);
-        cf_add_df(hy, ty);
-        cf_add_df(hz, tz);
-    }
-    ax += (double)hx.h + (double)hx.l;
-    ay += (double)hy.h + (double)hy.l;
-    az += (double)hz.h + (double)hz.l;
 }
 
 // Double-float (F64: FP64) field at an FP32 point from paired-layout

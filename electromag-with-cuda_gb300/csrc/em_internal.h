@@ -114,12 +114,12 @@ template <class T> struct ExtParams {
     int *err;
     // Tail hand-off.  Once the queue is dry and at most tail_lines lines are
     // still being traced, a kernel saves each of them (ExtCont) and stops;
-    // the wide kernel then traces them with `wide` warps per line, and hands
+    // a tail kernel then traces them with `wide` warps per line, and hands
     // them on again (to a wider launch) once few enough are left.
     // tail_lines = 0 turns the hand-off off.
     void *cont;                              // ExtCont<T> records written here
     unsigned long long *cont_count;          // ... and their count
-    const void *cont_in;                     // the wide kernel's lines
+    const void *cont_in;                     // the tail kernel's lines
     const unsigned long long *cont_in_count; // ... and their count
     unsigned long long *cont_next;           // input lines taken
     unsigned long long *live_count;          // lines neither finished nor handed off
@@ -127,7 +127,7 @@ template <class T> struct ExtParams {
     int wide;
 };
 
-// A line handed from the lane-group kernel to the wide kernel: its next row
+// A line handed from the lane-group kernel to a tail kernel: its next row
 // and limit, the evaluation point and the FP64 position accumulator.
 template <class T> struct ExtCont {
     long long line;
@@ -142,11 +142,11 @@ cudaError_t launch_ext_stage(const void *raw, int p, void *staged, int p_pad, in
 template <class T>
 cudaError_t launch_ext_trace(const ExtParams<T> &p, const struct LaunchCfg &cfg, int mode,
                              cudaStream_t stream);
-// The wide kernel over the handed-off lines (p.wide warps per line).
+// The tail kernels over the handed-off lines (p.wide warps per line).
 template <class T>
 cudaError_t launch_ext_wide(const ExtParams<T> &p, const struct LaunchCfg &cfg, int mode,
                             cudaStream_t stream);
-constexpr size_t kExtWideSlots = 4096; // static shared memory of the wide kernel (bound)
+constexpr size_t kExtWideSlots = 4096; // static shared memory of the tail kernels (bound)
 
 // Adjoint of the frozen-step map (em_adjoint.cu).
 struct AdjParams {

@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(ext_cta_threads(MODE), 1)
             }
         }
         // tail hand-off: with the queue dry, once few enough lines are left
-        // the warp's lines go to the wide kernel (warp-uniform decision)
+        // the warp's lines go to the tail kernels (warp-uniform decision)
         bool hand_off = false;
         if (tail_check) {
             const unsigned long long ns = __shfl_sync(0xffffffffu, next_seen, 0);
