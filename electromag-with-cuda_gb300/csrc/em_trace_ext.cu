@@ -971,6 +971,62 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
     }
 }
 
+// Four warp-wide reductions at once — sums of a, b, c and the minimum of d
+// — in six shuffles instead of twenty: at offsets 16 and 8 each lane hands
+// its partner the half of its values the partner keeps, then three full
+// levels; lane 8i ends with value i (a, b, c, d), as do the other lanes of
+// its block of eight.
+__device__ __forceinline__ float warp_reduce4(float a, float b, float c, float d, int lane)
+{
+    const unsigned FULL = 0xffffffffu;
+    const bool h16 = lane & 16, h8 = lane & 8;
+    float k0 = h16 ? c : a, k1 = h16 ? d : b;
+    const float r0 = __shfl_xor_sync(FULL, h16 ? a : c, 16);
+    const float r1 = __shfl_xor_sync(FULL, h16 ? b : d, 16);
+    k0 = k0 + r0;
+    k1 = h16 ? fminf(k1, r1) : k1 + r1;
+    float k = h8 ? k1 : k0;
+    const float r = __shfl_xor_sync(FULL, h8 ? k0 : k1, 8);
+    const bool mn = h16 && h8;
+    k = mn ? fminf(k, r) : k + r;
+#pragma unroll
+    for (int o = 4; o >= 1; o >>= 1) {
+        const float q = __shfl_xor_sync(FULL, k, o);
+        k = mn ? fminf(k, q) : k + q;
+    }
+    return k;
+}
+
+// The four totals over a group of 16 warps from their slots (x, y, z: sums;
+// w: minimum), in every lane, in nine shuffles: lanes l and l + 16 hold slot
+// l mod 16; offsets 8 and 4 trade halves, 2 and 1 finish, and each total is
+// read from a lane that holds it.  Every warp of the group gets the same
+// bits (the same operations on the same slots).
+__device__ __forceinline__ void slots_reduce16(float4 v, int lane, float &a, float &b, float &c,
+                                               float &d)
+{
+    const unsigned FULL = 0xffffffffu;
+    const bool h8 = lane & 8, h4 = lane & 4;
+    float k0 = h8 ? v.z : v.x, k1 = h8 ? v.w : v.y;
+    const float r0 = __shfl_xor_sync(FULL, h8 ? v.x : v.z, 8);
+    const float r1 = __shfl_xor_sync(FULL, h8 ? v.y : v.w, 8);
+    k0 = k0 + r0;
+    k1 = h8 ? fminf(k1, r1) : k1 + r1;
+    float k = h4 ? k1 : k0;
+    const float r = __shfl_xor_sync(FULL, h4 ? k0 : k1, 4);
+    const bool mn = h8 && h4;
+    k = mn ? fminf(k, r) : k + r;
+#pragma unroll
+    for (int o = 2; o >= 1; o >>= 1) {
+        const float q = __shfl_xor_sync(FULL, k, o);
+        k = mn ? fminf(k, q) : k + q;
+    }
+    a = __shfl_sync(FULL, k, 0);
+    b = __shfl_sync(FULL, k, 4);
+    c = __shfl_sync(FULL, k, 8);
+    d = __shfl_sync(FULL, k, 12);
+}
+
 // Barrier over the nthreads threads (whole warps) of one line group; id 1..15
 // (0 is the CTA barrier).
 __device__ __forceinline__ void group_barrier(int id, int nthreads)
@@ -995,7 +1051,7 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
     using Rec = typename ChargeRec<T>::type;
     constexpr int MW = kExtWideThreads / 32;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ T slots[2][MW][8];   // each warp's sums, by row parity
+    __shared__ __align__(16) T slots[2][MW][8]; // each warp's sums, by row parity
     __shared__ double rslots[MW][4]; // each warp's re-evaluation sums
     __shared__ long long grp_next[MW];
     __shared__ unsigned long long grp_live[2][MW];
@@ -1005,7 +1061,12 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
     // with FP64 parts (mixed position, double-float, FP64) run on the
     // group's first warp only: repeated in every warp they queue on the
     // FP64 pipe (mixed 18.4 -> 25.8 ms, double-float 47 -> 95 ms)
-    constexpr bool kAllStep = MODE == EXT_FAST && sizeof(T) == 4;
+    // (FP32, measured on the 4096-charge set with termination: every warp
+    // combining and stepping 8.9 ms, the first warp alone publishing 9.15;
+    // the four sums reduced together, 6 + 9 shuffles per warp and row
+    // instead of 20 + 20: 9.5 ms before)
+    constexpr bool kFp32 = MODE == EXT_FAST && sizeof(T) == 4;
+    constexpr bool kAllStep = kFp32;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     Rec *tiles = reinterpret_cast<Rec *>(smem + 128);
 
@@ -1093,7 +1154,20 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
                        CF &hz, double &Edx, double &Edy, double &Edz) {
         const bool mine = lane < W;
         const T *gs = slots[par][g * W + (mine ? lane : 0)];
-        if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+        if constexpr (kFp32) {
+            if (W == 16) {
+                const float4 v =
+                    *reinterpret_cast<const float4 *>(slots[par][g * W + (lane & 15)]);
+                slots_reduce16(v, lane, ax, ay, az, dneg);
+            } else {
+                ax = group_sum<T, 32>(mine ? gs[0] : T(0));
+                ay = group_sum<T, 32>(mine ? gs[1] : T(0));
+                az = group_sum<T, 32>(mine ? gs[2] : T(0));
+                dneg = group_min<T, 32>(mine ? gs[3] : T(3.0e38));
+            }
+            ext_field<T, MODE>(ax, ay, az, hx, hy, hz, Edx, Edy, Edz);
+            return;
+        } else if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
             hx.h = mine ? gs[0] : 0.0f;
             hx.l = mine ? gs[1] : 0.0f;
             hy.h = mine ? gs[2] : 0.0f;
@@ -1188,28 +1262,35 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
             group_two_sum<32>(hz);
             if constexpr (MODE == EXT_MIXED)
                 dall = group_sum<float, 32>(dall);
-        } else {
+        } else if constexpr (!kFp32) {
             ax = group_sum<T, 32>(ax);
             ay = group_sum<T, 32>(ay);
             az = group_sum<T, 32>(az);
         }
-        dneg = group_min<T, 32>(dneg);
-        if (lane == 0) {
-            T *o = slots[par][warp];
-            if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
-                o[0] = hx.h;
-                o[1] = hx.l;
-                o[2] = hy.h;
-                o[3] = hy.l;
-                o[4] = hz.h;
-                o[5] = hz.l;
-            } else {
-                o[0] = ax;
-                o[1] = ay;
-                o[2] = az;
+        if constexpr (kFp32) {
+            // FP32: the four sums at once; slot words 0..3 = x, y, z, dneg
+            const float k = warp_reduce4(ax, ay, az, dneg, lane);
+            if ((lane & 7) == 0)
+                slots[par][warp][lane >> 3] = k;
+        } else {
+            dneg = group_min<T, 32>(dneg);
+            if (lane == 0) {
+                T *o = slots[par][warp];
+                if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+                    o[0] = hx.h;
+                    o[1] = hx.l;
+                    o[2] = hy.h;
+                    o[3] = hy.l;
+                    o[4] = hz.h;
+                    o[5] = hz.l;
+                } else {
+                    o[0] = ax;
+                    o[1] = ay;
+                    o[2] = az;
+                }
+                o[6] = dneg;
+                o[7] = (T)dall;
             }
-            o[6] = dneg;
-            o[7] = (T)dall;
         }
         if (t == 0 && use_row)
             grp_live[par][g] = live_seen;
