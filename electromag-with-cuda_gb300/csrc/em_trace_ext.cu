@@ -585,6 +585,122 @@ __global__ void __launch_bounds__(ext_cta_threads(MODE), 1)
     }
 }
 
+// Four warp-wide reductions at once — sums of a, b, c and the minimum of d
+// — in six shuffles instead of twenty: at offsets 16 and 8 each lane hands
+// its partner the half of its values the partner keeps, then three full
+// levels; lane 8i ends with value i (a, b, c, d), as do the other lanes of
+// its block of eight.
+__device__ __forceinline__ float warp_reduce4(float a, float b, float c, float d, int lane)
+{
+    const unsigned FULL = 0xffffffffu;
+    const bool h16 = lane & 16, h8 = lane & 8;
+    float k0 = h16 ? c : a, k1 = h16 ? d : b;
+    const float r0 = __shfl_xor_sync(FULL, h16 ? a : c, 16);
+    const float r1 = __shfl_xor_sync(FULL, h16 ? b : d, 16);
+    k0 = k0 + r0;
+    k1 = h16 ? fminf(k1, r1) : k1 + r1;
+    float k = h8 ? k1 : k0;
+    const float r = __shfl_xor_sync(FULL, h8 ? k0 : k1, 8);
+    const bool mn = h16 && h8;
+    k = mn ? fminf(k, r) : k + r;
+#pragma unroll
+    for (int o = 4; o >= 1; o >>= 1) {
+        const float q = __shfl_xor_sync(FULL, k, o);
+        k = mn ? fminf(k, q) : k + q;
+    }
+    return k;
+}
+
+// The compensated modes' per-warp sums — three (hi, lo) sums X, Y, Z and an
+// item W of the nearest negative distance^2 (minimum) and sum q^2/r^4 — in
+// twelve shuffles instead of forty: at offsets 16 and 8 each lane hands its
+// partner the half of its items the partner keeps, then three full levels
+// with the operands ordered by lane half (both partners get the same bits);
+// lane 8i ends with item i as (f, g): (hi, lo), or (dneg, l2) for W.
+__device__ __forceinline__ void warp_reduce_cf(const CF &x, const CF &y, const CF &z, float dneg,
+                                               float l2, int lane, float &f, float &g)
+{
+    const unsigned FULL = 0xffffffffu;
+    auto cf = [](float ah, float al, float bh, float bl, float &h, float &l) {
+        float sum, err;
+        two_sum(ah, bh, sum, err);
+        h = sum;
+        l = __fadd_rn(__fadd_rn(al, bl), err);
+    };
+    const bool h16 = lane & 16, h8 = lane & 8;
+    // offset 16: the lower half keeps X and Y, the upper half Z and W
+    float k0h = h16 ? z.h : x.h, k0l = h16 ? z.l : x.l;
+    float k1h = h16 ? dneg : y.h, k1l = h16 ? l2 : y.l;
+    const float s0h = __shfl_xor_sync(FULL, h16 ? x.h : z.h, 16);
+    const float s0l = __shfl_xor_sync(FULL, h16 ? x.l : z.l, 16);
+    const float s1h = __shfl_xor_sync(FULL, h16 ? y.h : dneg, 16);
+    const float s1l = __shfl_xor_sync(FULL, h16 ? y.l : l2, 16);
+    cf(k0h, k0l, s0h, s0l, k0h, k0l);
+    if (h16) {
+        k1h = fminf(k1h, s1h);
+        k1l = __fadd_rn(k1l, s1l);
+    } else {
+        cf(k1h, k1l, s1h, s1l, k1h, k1l);
+    }
+    // offset 8: item i = 2 h16 + h8 stays
+    float ih = h8 ? k1h : k0h, il = h8 ? k1l : k0l;
+    const float rh = __shfl_xor_sync(FULL, h8 ? k0h : k1h, 8);
+    const float rl = __shfl_xor_sync(FULL, h8 ? k0l : k1l, 8);
+    const bool w = h16 && h8;
+    if (w) {
+        ih = fminf(ih, rh);
+        il = __fadd_rn(il, rl);
+    } else {
+        cf(ih, il, rh, rl, ih, il);
+    }
+#pragma unroll
+    for (int o = 4; o >= 1; o >>= 1) {
+        const float oh = __shfl_xor_sync(FULL, ih, o);
+        const float ol = __shfl_xor_sync(FULL, il, o);
+        const bool up = lane & o;
+        const float ah = up ? oh : ih, bh = up ? ih : oh;
+        const float al = up ? ol : il, bl = up ? il : ol;
+        if (w) {
+            ih = fminf(ah, bh);
+            il = __fadd_rn(al, bl);
+        } else {
+            cf(ah, al, bh, bl, ih, il);
+        }
+    }
+    f = ih;
+    g = il;
+}
+
+// The four totals over a group of 16 warps from their slots (x, y, z: sums;
+// w: minimum), in every lane, in nine shuffles: lanes l and l + 16 hold slot
+// l mod 16; offsets 8 and 4 trade halves, 2 and 1 finish, and each total is
+// read from a lane that holds it.  Every warp of the group gets the same
+// bits (the same operations on the same slots).
+__device__ __forceinline__ void slots_reduce16(float4 v, int lane, float &a, float &b, float &c,
+                                               float &d)
+{
+    const unsigned FULL = 0xffffffffu;
+    const bool h8 = lane & 8, h4 = lane & 4;
+    float k0 = h8 ? v.z : v.x, k1 = h8 ? v.w : v.y;
+    const float r0 = __shfl_xor_sync(FULL, h8 ? v.x : v.z, 8);
+    const float r1 = __shfl_xor_sync(FULL, h8 ? v.y : v.w, 8);
+    k0 = k0 + r0;
+    k1 = h8 ? fminf(k1, r1) : k1 + r1;
+    float k = h4 ? k1 : k0;
+    const float r = __shfl_xor_sync(FULL, h4 ? k0 : k1, 4);
+    const bool mn = h8 && h4;
+    k = mn ? fminf(k, r) : k + r;
+#pragma unroll
+    for (int o = 2; o >= 1; o >>= 1) {
+        const float q = __shfl_xor_sync(FULL, k, o);
+        k = mn ? fminf(k, q) : k + q;
+    }
+    a = __shfl_sync(FULL, k, 0);
+    b = __shfl_sync(FULL, k, 4);
+    c = __shfl_sync(FULL, k, 8);
+    d = __shfl_sync(FULL, k, 12);
+}
+
 // ---------------------------------------------------------------------------
 // The handed-off lines with streamed charges, W = P.wide warps per line (a
 // group); the groups of a CTA share the tile ring, so they step in
@@ -803,35 +919,31 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
                     mbar_arrive(empty0 + 8 * sg);
             }
         }
-        // ---- each warp's sums into the slots -------------------------------
+        // ---- each warp's sums into the slots (words 0..5 the field, 6 dneg,
+        // 7 l2), the values reduced together where they are FP32 words
         if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
-            group_two_sum<32>(hx);
-            group_two_sum<32>(hy);
-            group_two_sum<32>(hz);
-            if constexpr (MODE == EXT_MIXED)
-                dall = group_sum<float, 32>(dall);
+            float f, g2;
+            warp_reduce_cf(hx, hy, hz, dneg, dall, lane, f, g2);
+            if ((lane & 7) == 0) {
+                slots[warp][2 * (lane >> 3)] = f;
+                slots[warp][2 * (lane >> 3) + 1] = g2;
+            }
+        } else if constexpr (sizeof(T) == 4) {
+            const float k = warp_reduce4(ax, ay, az, dneg, lane);
+            if ((lane & 7) == 0)
+                slots[warp][lane == 24 ? 6 : lane >> 3] = k;
         } else {
             ax = group_sum<T, 32>(ax);
             ay = group_sum<T, 32>(ay);
             az = group_sum<T, 32>(az);
-        }
-        dneg = group_min<T, 32>(dneg);
-        if (lane == 0) {
-            T *o = slots[warp];
-            if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
-                o[0] = hx.h;
-                o[1] = hx.l;
-                o[2] = hy.h;
-                o[3] = hy.l;
-                o[4] = hz.h;
-                o[5] = hz.l;
-            } else {
+            dneg = group_min<T, 32>(dneg);
+            if (lane == 0) {
+                T *o = slots[warp];
                 o[0] = ax;
                 o[1] = ay;
                 o[2] = az;
+                o[6] = dneg;
             }
-            o[6] = dneg;
-            o[7] = (T)dall;
         }
         // a wait that gave up in any warp stops every group (CTA-uniform)
         if (__syncthreads_or(failed)) {
@@ -969,62 +1081,6 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_kernel(const ExtP
         if (refines)
             atomicAdd(P.refines, refines);
     }
-}
-
-// Four warp-wide reductions at once — sums of a, b, c and the minimum of d
-// — in six shuffles instead of twenty: at offsets 16 and 8 each lane hands
-// its partner the half of its values the partner keeps, then three full
-// levels; lane 8i ends with value i (a, b, c, d), as do the other lanes of
-// its block of eight.
-__device__ __forceinline__ float warp_reduce4(float a, float b, float c, float d, int lane)
-{
-    const unsigned FULL = 0xffffffffu;
-    const bool h16 = lane & 16, h8 = lane & 8;
-    float k0 = h16 ? c : a, k1 = h16 ? d : b;
-    const float r0 = __shfl_xor_sync(FULL, h16 ? a : c, 16);
-    const float r1 = __shfl_xor_sync(FULL, h16 ? b : d, 16);
-    k0 = k0 + r0;
-    k1 = h16 ? fminf(k1, r1) : k1 + r1;
-    float k = h8 ? k1 : k0;
-    const float r = __shfl_xor_sync(FULL, h8 ? k0 : k1, 8);
-    const bool mn = h16 && h8;
-    k = mn ? fminf(k, r) : k + r;
-#pragma unroll
-    for (int o = 4; o >= 1; o >>= 1) {
-        const float q = __shfl_xor_sync(FULL, k, o);
-        k = mn ? fminf(k, q) : k + q;
-    }
-    return k;
-}
-
-// The four totals over a group of 16 warps from their slots (x, y, z: sums;
-// w: minimum), in every lane, in nine shuffles: lanes l and l + 16 hold slot
-// l mod 16; offsets 8 and 4 trade halves, 2 and 1 finish, and each total is
-// read from a lane that holds it.  Every warp of the group gets the same
-// bits (the same operations on the same slots).
-__device__ __forceinline__ void slots_reduce16(float4 v, int lane, float &a, float &b, float &c,
-                                               float &d)
-{
-    const unsigned FULL = 0xffffffffu;
-    const bool h8 = lane & 8, h4 = lane & 4;
-    float k0 = h8 ? v.z : v.x, k1 = h8 ? v.w : v.y;
-    const float r0 = __shfl_xor_sync(FULL, h8 ? v.x : v.z, 8);
-    const float r1 = __shfl_xor_sync(FULL, h8 ? v.y : v.w, 8);
-    k0 = k0 + r0;
-    k1 = h8 ? fminf(k1, r1) : k1 + r1;
-    float k = h4 ? k1 : k0;
-    const float r = __shfl_xor_sync(FULL, h4 ? k0 : k1, 4);
-    const bool mn = h8 && h4;
-    k = mn ? fminf(k, r) : k + r;
-#pragma unroll
-    for (int o = 2; o >= 1; o >>= 1) {
-        const float q = __shfl_xor_sync(FULL, k, o);
-        k = mn ? fminf(k, q) : k + q;
-    }
-    a = __shfl_sync(FULL, k, 0);
-    b = __shfl_sync(FULL, k, 4);
-    c = __shfl_sync(FULL, k, 8);
-    d = __shfl_sync(FULL, k, 12);
 }
 
 // Barrier over the nthreads threads (whole warps) of one line group; id 1..15
@@ -1256,13 +1312,7 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
             tile_pairs<T, MODE>(32, tiles + pb, jn, pe - pb, lane, st, ax, ay, az, dneg, dall,
                                 hx, hy, hz);
         }
-        if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
-            group_two_sum<32>(hx);
-            group_two_sum<32>(hy);
-            group_two_sum<32>(hz);
-            if constexpr (MODE == EXT_MIXED)
-                dall = group_sum<float, 32>(dall);
-        } else if constexpr (!kFp32) {
+        if constexpr (!kFp32 && MODE != EXT_MIXED && MODE != EXT_DF64) {
             ax = group_sum<T, 32>(ax);
             ay = group_sum<T, 32>(ay);
             az = group_sum<T, 32>(az);
@@ -1272,6 +1322,15 @@ __global__ void __launch_bounds__(kExtWideThreads, 1) ext_wide_res_kernel(const 
             const float k = warp_reduce4(ax, ay, az, dneg, lane);
             if ((lane & 7) == 0)
                 slots[par][warp][lane >> 3] = k;
+        } else if constexpr (MODE == EXT_MIXED || MODE == EXT_DF64) {
+            // the compensated sums, dneg and l2 at once; slot words
+            // 2i, 2i + 1 = item i (hx, hy, hz, then dneg and l2)
+            float f, g2;
+            warp_reduce_cf(hx, hy, hz, dneg, dall, lane, f, g2);
+            if ((lane & 7) == 0) {
+                slots[par][warp][2 * (lane >> 3)] = f;
+                slots[par][warp][2 * (lane >> 3) + 1] = g2;
+            }
         } else {
             dneg = group_min<T, 32>(dneg);
             if (lane == 0) {
