@@ -175,21 +175,23 @@ int trace_lines(T *x, T *y, T *z, size_t n, size_t max_steps, const int32_t *spl
             }
         }
     }
-    // with resident charges a warp's share of a row must outweigh the two
-    // warp reductions and the barriers per row: at least 8 FP32 pairs per
-    // lane (about 14 instructions each), 6 mixed or double-float, 1 FP64
-    // (measured on the GPU-scale set with termination: 32 / 24 / 12 pairs
-    // gave 14.4 / 31.5 / 57 ms for FP32 / mixed / double-float, 16 / 12 / 6
-    // gave 12.8 / 25.7 / 54, 8 / 6 / 3 gave 12.0 / 23.0 / 55); below two
-    // warps per line the lane-group kernel's regrouping (a warp per line)
-    // serves the tail better.  Streamed rows also wait on the tile ring, so
-    // there the count alone sets W.
+    // with resident charges a warp's share of a row must outweigh the
+    // per-row reductions, the barrier and the step, which every warp of a
+    // group runs (FP32) or waits for: at least 16 FP32 pairs per lane
+    // (about 14 instructions each), 12 mixed, 6 double-float, 1 FP64
+    // (measured on the GPU-scale set with termination, resident-charge tail
+    // kernel: 8 / 6 pairs per lane (16 warps for a lone line) gave 8.9 /
+    // 15.7 ms for FP32 / mixed, 16 / 12 (8 warps) 8.8 / 15.3, 32 / 24 (4
+    // warps) 9.0 / 15.5; double-float at 6 pairs: 44.3 ms); below two warps
+    // per line the lane-group kernel's regrouping (a warp per line) serves
+    // the tail better.  Streamed rows also wait on the tile ring, so there
+    // the count alone sets W.
     int w_cap = wcfg.warps;
     if (cfg.resident) {
         const long long per_lane = sizeof(T) == 8       ? 1
                                    : mode == EXT_DF64  ? 6
-                                   : mode == EXT_MIXED ? 6
-                                                       : 8;
+                                   : mode == EXT_MIXED ? 12
+                                                       : 16;
         w_cap = (int)std::min<long long>(wcfg.warps, p_pad / (32LL * per_lane));
     }
     const bool tail = !o.deterministic && !o.warps_per_cta && w_cap >= 2 &&

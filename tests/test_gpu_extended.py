@@ -283,7 +283,7 @@ def test_mixed_refinement_in_df64_equals_fp64(em, gpu, ext_case):
 def tail_case(em, orc):
     """1023 lines of the 4096-charge workload (every 32nd seed): few enough
     that the lane-group kernel hands them all to the resident-charge tail
-    kernel, in rounds of 2, 4, 8 and 16 warps per line."""
+    kernel, in rounds of 2, 4 and 8 warps per line (16 in double-float)."""
     ch, seeds, _ = em.workloads.make("gpu_4096", seed=1234)
     seeds = seeds[::32].astype(np.float32)
     steps = 600
