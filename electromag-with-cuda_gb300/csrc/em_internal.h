@@ -269,6 +269,9 @@ struct LaunchCfg {
 
 // Charge padding granule per launch configuration (records).
 constexpr int kUnroll = 8;
+// CTA size cap of the exact arithmetic: one lane per line leaves few warps
+// per SM anyway, and eight pairs' terms in flight need the registers
+constexpr int kExactMaxThreads = 256;
 
 template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,

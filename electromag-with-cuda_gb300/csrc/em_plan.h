@@ -199,7 +199,10 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     const bool resident = !o.force_streamed && 128 + p_res * rec <= smem_cap;
     // the mixed form's per-line sums need more than 64 registers: at most
     // 512 threads (128 registers) per CTA
-    const int max_warps = (arith == ARITH_MIXED ? 16 : 32) - (resident ? 0 : 1);
+    const int max_warps = (arith == ARITH_MIXED   ? 16
+                           : arith == ARITH_EXACT ? kExactMaxThreads / 32
+                                                  : 32) -
+                          (resident ? 0 : 1);
     if (arith == ARITH_MIXED) {
         // the mixed form takes its groups from a queue, so rounds need no
         // balancing: 8 lanes x 2 lines (unless asked otherwise) and every

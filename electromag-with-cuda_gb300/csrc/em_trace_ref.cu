@@ -64,6 +64,36 @@ __device__ __forceinline__ void pair_exact(T px, T py, T pz, const C &c, T K, bo
     }
 }
 
+// The term of pair_exact (FP32), with the branch-free rounded root and
+// quotients: the same bits when it returns true (operands inside the checked
+// range: r^2 in [2^-40, 2^40] and every numerator in exact_range).
+template <class C>
+__device__ __forceinline__ bool pair_exact_nb(float px, float py, float pz, const C &c, float K,
+                                              bool three_arg, float &tx, float &ty, float &tz)
+{
+    const float rx = sub_rn(px, c.x), ry = sub_rn(py, c.y), rz = sub_rn(pz, c.z);
+    const float l2 = add_rn(add_rn(mul_rn(rx, rx), mul_rn(ry, ry)), mul_rn(rz, rz));
+    const float d = mul_rn(l2, sqrt_rn_nb(l2));
+    const float y = rcp_rn_nb(d);
+    bool ok = l2 >= 0x1p-40f && l2 <= 0x1p40f;
+    if (three_arg) {
+        const float nx = mul_rn(mul_rn(rx, K), c.q), ny = mul_rn(mul_rn(ry, K), c.q),
+                    nz = mul_rn(mul_rn(rz, K), c.q);
+        ok = ok && exact_range(nx) && exact_range(ny) && exact_range(nz);
+        tx = div_rn_nb(nx, d, y);
+        ty = div_rn_nb(ny, d, y);
+        tz = div_rn_nb(nz, d, y);
+    } else {
+        const float n0 = mul_rn(K, c.q);
+        ok = ok && exact_range(n0);
+        const float s = div_rn_nb(n0, d, y);
+        tx = mul_rn(rx, s);
+        ty = mul_rn(ry, s);
+        tz = mul_rn(rz, s);
+    }
+    return ok;
+}
+
 // Per-line field accumulator: scalar components, plus packed pairs for the
 // .f32x2 path (kept across charge tiles so tiling never changes the sum).
 template <class T> struct Acc {
@@ -89,11 +119,39 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
 #pragma unroll kUnroll
         for (int j = t; j < count; j += TPL)
             pair_fast<T>(px, py, pz, load_charge(tile, j), a.x, a.y, a.z);
+    } else if constexpr (sizeof(T) == 4) {
+        // one lane per line (the reference's charge order): the terms of
+        // consecutive charges are independent, only the sums are ordered.
+        // Eight terms at a time from the branch-free rounded operations (the
+        // same bits), a rare pass redoing any term whose operands leave
+        // their checked range, then the eight sums in charge order; count
+        // is a multiple of 8 (the padding granule).
+        for (int j0 = t; j0 < count; j0 += 8 * TPL) {
+            T tx[8], ty[8], tz[8];
+            bool ok = true;
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                ok &= pair_exact_nb(px, py, pz, load_charge(tile, j0 + u * TPL), K, three_arg,
+                                    tx[u], ty[u], tz[u]);
+            if (!ok) {
+                for (int u = 0; u < 8; ++u) {
+                    T ex = 0, ey = 0, ez = 0;
+                    pair_exact<T>(px, py, pz, load_charge(tile, j0 + u * TPL), K, three_arg,
+                                  ex, ey, ez);
+                    tx[u] = ex;
+                    ty[u] = ey;
+                    tz[u] = ez;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                a.x = add_rn(a.x, tx[u]);
+                a.y = add_rn(a.y, ty[u]);
+                a.z = add_rn(a.z, tz[u]);
+            }
+        }
     } else {
-        // one lane per line (the reference's charge order): the rounded
-        // divides and roots of consecutive charges are independent, only the
-        // sums are ordered, so a deep unroll keeps several pairs in flight
-#pragma unroll(sizeof(T) == 4 ? 8 : 2)
+#pragma unroll 2
         for (int j = t; j < count; j += TPL)
             pair_exact<T>(px, py, pz, load_charge(tile, j), K, three_arg, a.x, a.y, a.z);
     }
@@ -688,7 +746,7 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &params, const LaunchCfg &c
     if (arith == ARITH_EXACT) {
         if (cfg.tpl != 1)
             return cudaErrorInvalidValue;
-        return launch_one<T, 1, ARITH_EXACT, 1, 1024>(p, cfg, stream);
+        return launch_one<T, 1, ARITH_EXACT, 1, kExactMaxThreads>(p, cfg, stream);
     }
     if (arith == ARITH_MIXED) {
         if constexpr (sizeof(T) != 4) {
