@@ -90,6 +90,7 @@ _SIGNATURES = {
     "em_field_f32": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_field_f64": (I, [P, P, P, S, P, S, P, P, P, P]),
     "em_fp32_peak_tflops": (I, [P, P]),
+    "em_selftest_rounded_ops": (I, [ctypes.c_ulonglong, P]),
     "em_selftest_wait_timeout": (I, [I, P]),
     "em_launch_count": (ctypes.c_ulonglong, []),
     "em_device_count": (I, []),

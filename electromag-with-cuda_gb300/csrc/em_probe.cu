@@ -1,10 +1,13 @@
 // Device diagnostics: the FP32 FFMA throughput of the current device (the
-// denominator of the tracer's FP32 roofline) and the count of kernels this
-// library has launched in the process.
+// denominator of the tracer's FP32 roofline), the count of kernels this
+// library has launched in the process, and self-checks (the bounded device
+// wait; the branch-free rounded operations of the exact arithmetic against
+// the compiler's rounded operations).
 #include <atomic>
 
 #include "em_device.cuh"
 #include "em_internal.h"
+#include "em_math.cuh"
 #include "emgb300.h"
 
 namespace em {
@@ -52,10 +55,83 @@ __global__ void wait_selftest_kernel(int *err, unsigned long long limit_ns)
     mbar_wait_limit(b, 0, err, limit_ns);
 }
 
+// The exact arithmetic's branch-free root, reciprocal and quotient against
+// __fsqrt_rn, __frcp_rn and __fdiv_rn over the operand ranges it admits:
+// every float in [2^-40, 2^40] (roots), every float in [2^-60, 2^60]
+// (divisors), and n quotients of a numerator and divisor with seeded random
+// significands, exponents in [-60, 60] and signs.  bad[0..2]: mismatches.
+__device__ __forceinline__ unsigned long long selftest_mix(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void rounded_ops_kernel(unsigned long long n, unsigned long long *bad)
+{
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long i0 = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    unsigned long long b0 = 0, b1 = 0, b2 = 0;
+    // bit patterns: 2^-40 .. 2^40 and 2^-60 .. 2^60 (positive, normal)
+    const unsigned r_lo = (127u - 40u) << 23, r_hi = (127u + 40u) << 23;
+    const unsigned d_lo = (127u - 60u) << 23, d_hi = (127u + 60u) << 23;
+    for (unsigned long long u = d_lo + i0; u <= d_hi; u += stride) {
+        const float x = __uint_as_float((unsigned)u);
+        if (u >= r_lo && u <= r_hi)
+            b0 += __float_as_uint(sqrt_rn_nb(x)) != __float_as_uint(__fsqrt_rn(x));
+        b1 += __float_as_uint(rcp_rn_nb(x)) != __float_as_uint(__frcp_rn(x));
+    }
+    for (unsigned long long i = i0; i < n; i += stride) {
+        const unsigned long long h = selftest_mix(i ^ 0x5eed5eed5eedull);
+        const unsigned ma = (unsigned)(h & 0x7fffff), mb = (unsigned)((h >> 23) & 0x7fffff);
+        const unsigned ea = (unsigned)((h >> 46) % 121) + 67u, eb = (unsigned)((h >> 54) % 121) + 67u;
+        const unsigned sa = (unsigned)(h >> 62) & 1u, sb = (unsigned)(h >> 63) & 1u;
+        const float a = __uint_as_float((sa << 31) | (ea << 23) | ma);
+        const float b = __uint_as_float((sb << 31) | (eb << 23) | mb);
+        b2 += __float_as_uint(div_rn_nb(a, b, rcp_rn_nb(b))) != __float_as_uint(__fdiv_rn(a, b));
+    }
+    if (b0)
+        atomicAdd(&bad[0], b0);
+    if (b1)
+        atomicAdd(&bad[1], b1);
+    if (b2)
+        atomicAdd(&bad[2], b2);
+}
+
 } // namespace
 } // namespace em
 
 extern "C" {
+
+int em_selftest_rounded_ops(unsigned long long n_quotients, unsigned long long *mismatches)
+{
+    if (!mismatches)
+        return EM_ERR_ARG;
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_NO_DEVICE;
+    }
+    unsigned long long *bad = nullptr;
+    if (cudaMalloc(&bad, 3 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_NOMEM;
+    }
+    cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
+    em::rounded_ops_kernel<<<prop.multiProcessorCount * 8, 256>>>(n_quotients, bad);
+    em::count_launch(1);
+    const cudaError_t e = cudaMemcpy(mismatches, bad, 3 * sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return EM_ERR_CUDA;
+    }
+    return EM_OK;
+}
+
 
 int em_selftest_wait_timeout(int limit_ms, double *elapsed_ms)
 {

@@ -463,6 +463,15 @@ EM_API int em_fp32_peak_tflops(double *tflops, double *seconds);
  * wait expired and the kernel returned as designed (the device stays
  * usable); *elapsed_ms gets the kernel's duration. */
 EM_API int em_selftest_wait_timeout(int limit_ms, double *elapsed_ms);
+/* Self-check of the exact arithmetic's branch-free correctly rounded
+ * operations against the compiler's rounded ones, over the operand ranges
+ * the exact tracer admits (other operands take the rounded operations):
+ * every float in [2^-40, 2^40] for the square root, every float in
+ * [2^-60, 2^60] for the reciprocal, and n_quotients seeded random quotients
+ * of operands in [2^-60, 2^60].  mismatches[0..2]: root, reciprocal,
+ * quotient mismatches (all zero when the operations agree bit for bit). */
+EM_API int em_selftest_rounded_ops(unsigned long long n_quotients,
+                                   unsigned long long *mismatches);
 EM_API unsigned long long em_launch_count(void);
 /* Library version, "major.minor.patch". */
 EM_API const char *em_version(void);
