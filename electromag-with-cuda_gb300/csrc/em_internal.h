@@ -269,9 +269,18 @@ struct LaunchCfg {
 
 // Charge padding granule per launch configuration (records).
 constexpr int kUnroll = 8;
-// CTA size cap of the exact arithmetic: one lane per line leaves few warps
-// per SM anyway, and eight pairs' terms in flight need the registers
-constexpr int kExactMaxThreads = 256;
+// The exact arithmetic: lanes per line in FP32 (their terms are added in
+// the reference's charge order by every lane of the line; FP64 keeps one
+// lane per line) — 8 while every line fits one round of 512-thread CTAs at
+// 8 lanes, else 4 (the reference's default run, 16 384 lines: 137 ms at 4
+// lanes, 169 at 8; 1088 lines: 17.8 ms at 4, 11.9 at 8) — and the CTA size
+// cap for a shape: one lane per line (16 terms in flight) needs the
+// registers of 256-thread CTAs, several lanes per line (8 in flight) fit 512
+constexpr int exact_max_threads(int tpl) { return tpl == 1 ? 256 : 512; }
+inline int exact_tpl_f32(long long n, int nsm)
+{
+    return n <= (long long)nsm * (exact_max_threads(8) / 32) * (32 / 8) ? 8 : 4;
+}
 
 template <class T>
 cudaError_t launch_ref_trace(const RefTraceParams<T> &p, const LaunchCfg &cfg, int arith,

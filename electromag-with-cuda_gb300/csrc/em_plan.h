@@ -157,7 +157,9 @@ template <class T>
 int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl)
 {
     const size_t rec = sizeof(T) * 4;
-    const int fixed_tpl = o.arith == EM_ARITH_EXACT ? 1 : o.threads_per_line;
+    const int fixed_tpl = o.arith == EM_ARITH_EXACT
+                              ? (sizeof(T) == 4 ? exact_tpl_f32((long long)n, c.nsm) : 1)
+                              : o.threads_per_line;
     if (fixed_tpl != 0 && fixed_tpl != 1 && fixed_tpl != 2 && fixed_tpl != 4 && fixed_tpl != 8)
         return EM_ERR_ARG;
     // tile overrides beyond 65 536 records could never fit shared memory and
@@ -200,7 +202,7 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
     // the mixed form's per-line sums need more than 64 registers: at most
     // 512 threads (128 registers) per CTA
     const int max_warps = (arith == ARITH_MIXED   ? 16
-                           : arith == ARITH_EXACT ? kExactMaxThreads / 32
+                           : arith == ARITH_EXACT ? exact_max_threads(fixed_tpl) / 32
                                                   : 32) -
                           (resident ? 0 : 1);
     if (arith == ARITH_MIXED) {

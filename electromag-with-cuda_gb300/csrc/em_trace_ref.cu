@@ -120,6 +120,42 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
 #pragma unroll kUnroll
         for (int j = t; j < count; j += TPL)
             pair_fast<T>(px, py, pz, load_charge(tile, j), a.x, a.y, a.z);
+    } else if constexpr (sizeof(T) == 4 && TPL > 1) {
+        // TPL lanes per line: lane t forms the terms of charges j0 + u TPL + t
+        // (eight per lane in flight, from the branch-free rounded operations,
+        // redone with the compiler's rounded operations when an operand
+        // leaves its checked range); each round's TPL terms are broadcast from
+        // their lanes and every lane of the line adds them in charge order,
+        // so all of them hold the reference's sum (no reduction after).
+        // count is a multiple of 8 TPL (the padding granule).
+        const int base = (threadIdx.x & 31) & ~(TPL - 1);
+        for (int j0 = 0; j0 < count; j0 += 8 * TPL) {
+            T tx[8], ty[8], tz[8];
+            bool ok = true;
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                ok &= pair_exact_nb(px, py, pz, load_charge(tile, j0 + u * TPL + t), K, three_arg,
+                                    tx[u], ty[u], tz[u]);
+            if (!ok) {
+                for (int u = 0; u < 8; ++u) {
+                    T ex = 0, ey = 0, ez = 0;
+                    pair_exact<T>(px, py, pz, load_charge(tile, j0 + u * TPL + t), K, three_arg,
+                                  ex, ey, ez);
+                    tx[u] = ex;
+                    ty[u] = ey;
+                    tz[u] = ez;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+#pragma unroll
+                for (int k = 0; k < TPL; ++k) {
+                    a.x = add_rn(a.x, __shfl_sync(0xffffffffu, tx[u], base + k));
+                    a.y = add_rn(a.y, __shfl_sync(0xffffffffu, ty[u], base + k));
+                    a.z = add_rn(a.z, __shfl_sync(0xffffffffu, tz[u], base + k));
+                }
+            }
+        }
     } else if constexpr (sizeof(T) == 4) {
         // one lane per line (the reference's charge order): the terms of
         // consecutive charges are independent, only the sums are ordered.
@@ -618,7 +654,8 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
             for (int k = 0; k < KL; ++k) {
                 acc_finish<T, ARITH>(acc[k]);
                 T ax = acc[k].x, ay = acc[k].y, az = acc[k].z;
-                if (TPL > 1) {
+                // (the exact arithmetic's lanes already hold the line's sum)
+                if (TPL > 1 && ARITH != ARITH_EXACT) {
                     ax = line_reduce<T, TPL>(ax);
                     ay = line_reduce<T, TPL>(ay);
                     az = line_reduce<T, TPL>(az);
@@ -753,9 +790,15 @@ cudaError_t launch_ref_trace(const RefTraceParams<T> &params, const LaunchCfg &c
     if (cfg.kl != 1 && (cfg.kl != 2 || arith == ARITH_EXACT))
         return cudaErrorInvalidValue;
     if (arith == ARITH_EXACT) {
-        if (cfg.tpl != 1)
-            return cudaErrorInvalidValue;
-        return launch_one<T, 1, ARITH_EXACT, 1, kExactMaxThreads>(p, cfg, stream);
+        if (cfg.tpl == 1)
+            return launch_one<T, 1, ARITH_EXACT, 1, exact_max_threads(1)>(p, cfg, stream);
+        if constexpr (sizeof(T) == 4) {
+            if (cfg.tpl == 4)
+                return launch_one<T, 4, ARITH_EXACT, 1, exact_max_threads(4)>(p, cfg, stream);
+            if (cfg.tpl == 8)
+                return launch_one<T, 8, ARITH_EXACT, 1, exact_max_threads(8)>(p, cfg, stream);
+        }
+        return cudaErrorInvalidValue;
     }
     if (arith == ARITH_MIXED) {
         if constexpr (sizeof(T) != 4) {

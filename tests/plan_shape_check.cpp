@@ -38,10 +38,18 @@ int main()
     expect("16384x1024 kl forced", make_plan<float>(c, 16384, 1024, o, &p) == EM_OK &&
                                        p.cfg.kl == 2);
     o.lines_per_thread = 0;
-    // exact arithmetic: one lane per line, one line per lane
+    // exact arithmetic: FP32 with 4 lanes per line for many lines, 8 for
+    // few (terms added in charge order by every lane), FP64 one lane per
+    // line; one line per lane, CTAs within the exact form's cap
     o.arith = EM_ARITH_EXACT;
-    expect("exact", make_plan<float>(c, 16384, 1024, o, &p) == EM_OK && p.cfg.tpl == 1 &&
-                        p.cfg.kl == 1 && p.arith == ARITH_EXACT);
+    expect("exact", make_plan<float>(c, 16384, 1024, o, &p) == EM_OK &&
+                        p.cfg.tpl == exact_tpl_f32(16384, c.nsm) && p.cfg.kl == 1 &&
+                        p.cfg.warps <= exact_max_threads(p.cfg.tpl) / 32 &&
+                        p.arith == ARITH_EXACT);
+    expect("exact few lines", make_plan<float>(c, 1088, 256, o, &p) == EM_OK &&
+                                  p.cfg.tpl == exact_tpl_f32(1088, c.nsm));
+    expect("exact f64", make_plan<double>(c, 16384, 1024, o, &p) == EM_OK && p.cfg.tpl == 1 &&
+                            p.cfg.kl == 1 && p.cfg.warps <= exact_max_threads(1) / 32);
     // mixed: 8 lanes x 2 lines, every warp of a 512-thread CTA the groups
     // keep busy (groups come from a queue: no round balancing)
     o.arith = EM_ARITH_MIXED;

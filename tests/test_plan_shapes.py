@@ -24,4 +24,4 @@ def test_planner_shapes(tmp_path):
                            "-o", str(exe)])
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("ok ") == 10
+    assert r.stdout.count("ok ") == 12
