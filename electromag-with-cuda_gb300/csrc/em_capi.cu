@@ -232,6 +232,8 @@ int calc_field(T *x, T *y, T *z, size_t n, size_t total_steps, const T *charges,
     const double kappa = mix_kappa(o);
     prm.kappa2 = kappa * kappa;
     prm.refines = refines;
+    if (pl.arith == ARITH_EXACT && sizeof(T) == 4)
+        prm.exact_nb = exact_nb_verified(s) ? 1 : 0;
     // the mixed form's groups come from a queue (status word at byte 40)
     if (pl.arith == ARITH_MIXED)
         prm.group_ctr = reinterpret_cast<unsigned long long *>(

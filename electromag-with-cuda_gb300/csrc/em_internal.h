@@ -72,7 +72,18 @@ template <class T> struct RefTraceParams {
     // optional (resident charges only): a zeroed counter from which warps
     // take line groups in order instead of the fixed round-robin deal
     unsigned long long *group_ctr;
+    // exact arithmetic (FP32): 1 when the branch-free rounded operations
+    // were verified on this device (exact_nb_verified), else 0 (the
+    // compiler's rounded operations)
+    int exact_nb;
 };
+
+// The exact arithmetic's branch-free rounded operations checked once per
+// device and process against the compiler's rounded operations
+// (em_probe.cu; every admitted root operand and divisor and 2^24 random
+// quotients, a few milliseconds on stream s, no allocation): true when they
+// agree bit for bit.
+bool exact_nb_verified(cudaStream_t s);
 
 // Extended tracer (em_trace_ext.cu).
 enum ExtMode : int {

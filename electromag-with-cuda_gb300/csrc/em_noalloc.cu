@@ -145,6 +145,8 @@ extern "C" int em_calc_field_noalloc_f32(float *x, float *y, float *z, size_t n,
     prm.rule = use_curvature ? RULE_SSE : RULE_FIXED;
     prm.resolution = resolution;
     prm.err = err;
+    if (pl.arith == ARITH_EXACT)
+        prm.exact_nb = exact_nb_verified(s) ? 1 : 0;
     if (e == cudaSuccess)
         e = launch_ref_trace<float>(prm, pl.cfg, pl.arith, s);
     int dev_err = 0;

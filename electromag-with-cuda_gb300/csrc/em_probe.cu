@@ -4,6 +4,7 @@
 // wait; the branch-free rounded operations of the exact arithmetic against
 // the compiler's rounded operations).
 #include <atomic>
+#include <mutex>
 
 #include "em_device.cuh"
 #include "em_internal.h"
@@ -99,7 +100,62 @@ __global__ void rounded_ops_kernel(unsigned long long n, unsigned long long *bad
         atomicAdd(&bad[2], b2);
 }
 
+// the check's counters: a static array, so the check allocates nothing
+__device__ unsigned long long g_rounded_bad[3];
+std::mutex g_rounded_mu;
+
+// Runs the check on stream s (serialised: one set of counters per device).
+cudaError_t run_rounded_check(unsigned long long n_quotients, unsigned long long *out,
+                              cudaStream_t s)
+{
+    std::lock_guard<std::mutex> guard(g_rounded_mu);
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    void *bad = nullptr;
+    if (e == cudaSuccess)
+        e = cudaGetSymbolAddress(&bad, g_rounded_bad);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(bad, 0, 3 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        rounded_ops_kernel<<<nsm * 8, 256, 0, s>>>(n_quotients,
+                                                   static_cast<unsigned long long *>(bad));
+        count_launch(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, bad, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    return e;
+}
+
 } // namespace
+
+bool exact_nb_verified(cudaStream_t s)
+{
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> state[kMaxDev]; // 0 unknown, 1 verified, 2 not
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+        cudaGetLastError();
+        return false;
+    }
+    const int v = state[dev].load();
+    if (v)
+        return v == 1;
+    unsigned long long bad[3] = {1, 1, 1};
+    const cudaError_t e = run_rounded_check(1ull << 24, bad, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false; // not verified: the compiler's rounded operations
+    }
+    const bool ok = bad[0] == 0 && bad[1] == 0 && bad[2] == 0;
+    state[dev].store(ok ? 1 : 2);
+    return ok;
+}
+
 } // namespace em
 
 extern "C" {
@@ -109,23 +165,11 @@ int em_selftest_rounded_ops(unsigned long long n_quotients, unsigned long long *
     if (!mismatches)
         return EM_ERR_ARG;
     int dev = 0;
-    cudaDeviceProp prop;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return EM_ERR_NO_DEVICE;
     }
-    unsigned long long *bad = nullptr;
-    if (cudaMalloc(&bad, 3 * sizeof(unsigned long long)) != cudaSuccess) {
-        cudaGetLastError();
-        return EM_ERR_NOMEM;
-    }
-    cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
-    em::rounded_ops_kernel<<<prop.multiProcessorCount * 8, 256>>>(n_quotients, bad);
-    em::count_launch(1);
-    const cudaError_t e = cudaMemcpy(mismatches, bad, 3 * sizeof(unsigned long long),
-                                     cudaMemcpyDeviceToHost);
-    cudaFree(bad);
-    if (e != cudaSuccess) {
+    if (em::run_rounded_check(n_quotients, mismatches, 0) != cudaSuccess) {
         cudaGetLastError();
         return EM_ERR_CUDA;
     }

@@ -105,7 +105,7 @@ template <class T> struct Acc {
 // Adds the charges held in shared memory [0, count) to lane t's partial sum.
 template <class T, int TPL, int ARITH, class Rec>
 __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T px, T py, T pz,
-                                           T K, bool three_arg, Acc<T> &a)
+                                           T K, bool three_arg, bool nb, Acc<T> &a)
 {
     if (ARITH == ARITH_FAST2) {
         // charge pairs t, t+TPL, ... ; count is a multiple of 2*TPL; the tile
@@ -131,11 +131,13 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
         const int base = (threadIdx.x & 31) & ~(TPL - 1);
         for (int j0 = 0; j0 < count; j0 += 8 * TPL) {
             T tx[8], ty[8], tz[8];
-            bool ok = true;
+            bool ok = nb;
+            if (nb) {
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
-                ok &= pair_exact_nb(px, py, pz, load_charge(tile, j0 + u * TPL + t), K, three_arg,
-                                    tx[u], ty[u], tz[u]);
+                for (int u = 0; u < 8; ++u)
+                    ok &= pair_exact_nb(px, py, pz, load_charge(tile, j0 + u * TPL + t), K,
+                                        three_arg, tx[u], ty[u], tz[u]);
+            }
             if (!ok) {
                 for (int u = 0; u < 8; ++u) {
                     T ex = 0, ey = 0, ez = 0;
@@ -168,11 +170,13 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
         auto batch = [&](int j0, auto bn) {
             constexpr int B = decltype(bn)::value;
             T tx[B], ty[B], tz[B];
-            bool ok = true;
+            bool ok = nb;
+            if (nb) {
 #pragma unroll
-            for (int u = 0; u < B; ++u)
-                ok &= pair_exact_nb(px, py, pz, load_charge(tile, j0 + u * TPL), K, three_arg,
-                                    tx[u], ty[u], tz[u]);
+                for (int u = 0; u < B; ++u)
+                    ok &= pair_exact_nb(px, py, pz, load_charge(tile, j0 + u * TPL), K,
+                                        three_arg, tx[u], ty[u], tz[u]);
+            }
             if (!ok) {
                 for (int u = 0; u < B; ++u) {
                     T ex = 0, ey = 0, ez = 0;
@@ -222,7 +226,7 @@ __device__ __forceinline__ void acc_finish(Acc<T> &a)
 template <class T, int TPL, int ARITH, int KL, class Rec>
 __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, const T *px,
                                              const T *py, const T *pz, T K, bool three_arg,
-                                             Acc<T> *a)
+                                             bool nb, Acc<T> *a)
 {
     if (ARITH == ARITH_FAST2 && KL > 1) {
         // a charge pair (two LDS.128) feeds KL lines, two charges per
@@ -244,7 +248,7 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
                 pair2_fast(PX[k], PY[k], PZ[k], A, B, a[k].X, a[k].Y, a[k].Z);
         }
     } else if (KL == 1) {
-        accumulate<T, TPL, ARITH>(tile, count, t, px[0], py[0], pz[0], K, three_arg, a[0]);
+        accumulate<T, TPL, ARITH>(tile, count, t, px[0], py[0], pz[0], K, three_arg, nb, a[0]);
     } else {
 #pragma unroll 8
         for (int j = t; j < count; j += TPL) {
@@ -520,6 +524,9 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
     const T K = (T)kElectroK;
     const bool curvature = P.rule != RULE_FIXED;
     const bool three_arg = P.rule == RULE_SSE;
+    // exact arithmetic: the branch-free rounded operations once verified on
+    // this device (else the compiler's rounded operations for every pair)
+    const bool nb = ARITH == ARITH_EXACT && P.exact_nb != 0;
     const int t = lane % TPL;
     const size_t n = (size_t)P.n;
 
@@ -621,7 +628,7 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                                               reinterpret_cast<const float *>(pz), hx, hy, hz,
                                               l2);
                 else
-                    accumulate_k<T, TPL, ARITH, KL>(tp, count, t, px, py, pz, K, three_arg,
+                    accumulate_k<T, TPL, ARITH, KL>(tp, count, t, px, py, pz, K, three_arg, nb,
                                                     acc);
             };
             if (!streamed) {
