@@ -60,7 +60,7 @@ def parse():
                     help="skip the single-GPU blocks of the other workloads "
                          "(always skipped when N > 1)")
     ap.add_argument("--case", choices=["ref-mixed", "ext-fp32", "ext-mixed", "ext-df64",
-                                       "ext-tail-dipole", "ext-tail-gpu", "adjoint",
+                                       "ext-tail-dipole", "ext-tail-gpu", "exact", "adjoint",
                                        "adjoint-checkpoint", "adjoint-twopass",
                                        "batch", "verlet"],
                     default=None,
@@ -234,7 +234,8 @@ def run_case(args):
     double-float pairs), the extended tracer with its tail kernel on the
     dipole set (1000 rows, termination radius 0.5) or on the 4096-charge
     workload (5000 rows, termination radius 0.5: lines that escape the
-    charges run all rows, on the tail kernel), the adjoint
+    charges run all rows, on the tail kernel), the reference's arithmetic
+    bit for bit on the 256-charge configuration (500 rows), the adjoint
     kernels on the 1024-charge workload (200 rows; stored field, or the
     field recomputed per 64-row segment; adjoint-twopass: 6000 charges, the
     two-pass backward of sets above 4096 charges), the batched tracer on the
@@ -284,6 +285,24 @@ def run_case(args):
         out = em.trace_lines(s, ch, 1000, 1.0, 0.5)
         torch.cuda.synchronize()
         print("tail", out["perf"].pairs / out["perf"].time / 1e9, "Gpair/s")
+        return 0
+    if args.case == "exact":
+        # the reference's arithmetic bit for bit, on the CPU-runnable
+        # configuration (256 charges, 1088 lines; --rows, default 500)
+        ch, seeds, _ = em.workloads.make("cpu_256", seed=args.seed)
+        rows = args.rows or 500
+        n = len(seeds)
+        chd = torch.from_numpy(np.ascontiguousarray(ch, np.float32)).to(dev)
+        V = torch.zeros((3, rows, n), dtype=torch.float32, device=dev)
+        V[:, 0, :] = torch.from_numpy(np.ascontiguousarray(seeds.T, np.float32)).to(dev)
+        for _ in range(2):
+            W = V.clone()
+            rc, perf = em.calc_field(W[0].reshape(-1), W[1].reshape(-1), W[2].reshape(-1),
+                                     chd, n, 1.0, True, arith="exact", require_n64=False)
+            if rc:
+                raise em.EmError(rc, "exact")
+        torch.cuda.synchronize()
+        print("exact", n * (rows - 1) * len(ch) / perf.time / 1e9, "Gpair/s")
         return 0
     if args.case == "ext-tail-gpu":
         ch, seeds, _ = em.workloads.make("gpu_4096", seed=args.seed)
