@@ -94,7 +94,10 @@ typedef struct em_options {
     int device_ptrs;  /* 1: x, y, z and charges are device pointers          */
     void *stream;     /* cudaStream_t for device_ptrs calls (NULL: the
                          library's stream, call returns when done)           */
-    int threads_per_line; /* 0: automatic; else 1, 2, 4 or 8                 */
+    int threads_per_line; /* 0: automatic; else 1, 2, 4 or 8 (the exact
+                             arithmetic sets its own: 4 or 8 lanes per line
+                             in FP32, adding the terms in the reference's
+                             order, 1 in FP64)                              */
     int warps_per_cta;    /* 0: automatic; else 1..32                        */
     int tile_charges;     /* 0: automatic; streamed-charge tile size         */
     int force_streamed;   /* 1: stream charge tiles even if they fit          */
