@@ -288,6 +288,13 @@ constexpr int kUnroll = 8;
 // cap for a shape: one lane per line (16 terms in flight) needs the
 // registers of 256-thread CTAs, several lanes per line (8 in flight) fit 512
 constexpr int exact_max_threads(int tpl) { return tpl == 1 ? 256 : 512; }
+// 8 lanes per line pass each round's terms through shared memory (eight
+// float4 per lane, after the charge tiles, every warp of a CTA); 4 lanes
+// broadcast them by shuffles (measured: 8 lanes 11.9 -> 11.1 ms on the
+// 256-charge configuration with the buffer, 4 lanes 136 -> 151 ms on the
+// reference's default run)
+constexpr int kExactSmemTpl = 8;
+constexpr size_t kExactTermBytesPerWarp = 32 * 8 * 16;
 inline int exact_tpl_f32(long long n, int nsm)
 {
     return n <= (long long)nsm * (exact_max_threads(8) / 32) * (32 / 8) ? 8 : 4;

@@ -193,7 +193,13 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
         fixed_kl = o.lines_per_thread ? o.lines_per_thread : 2;
     else if (arith == ARITH_FAST2)
         fixed_kl = o.lines_per_thread ? o.lines_per_thread : 2;
-    const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024);
+    // the exact arithmetic with several lanes per line keeps each warp's
+    // terms in shared memory beside the charges (up to a full CTA's warps)
+    const size_t term_bytes = arith == ARITH_EXACT && fixed_tpl >= kExactSmemTpl
+                                  ? (size_t)(exact_max_threads(fixed_tpl) / 32) *
+                                        kExactTermBytesPerWarp
+                                  : 0;
+    const size_t smem_cap = std::min<size_t>(c.smem_optin, 227 * 1024) - term_bytes;
     int tpl = 1, kl = 1, warps = 1;
     // resident if the padded set fits next to the barrier block
     const size_t gran_max = 16 * kUnroll;
@@ -238,7 +244,7 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
         r.n_tiles = 1;
         r.cfg.stages = 1;
         r.cfg.tile_recs = r.p_pad;
-        r.cfg.smem = 128 + (size_t)r.p_pad * rec;
+        r.cfg.smem = 128 + (size_t)r.p_pad * rec + term_bytes;
     } else {
         int tile = o.tile_charges ? o.tile_charges : (rec == 16 ? 1024 : 512);
         tile = (tile + gran - 1) / gran * gran;
@@ -252,7 +258,7 @@ int make_plan(const DevCtx &c, size_t n, size_t p, const em_options &o, Plan *pl
             r.n_tiles = 1;
         r.p_pad = r.n_tiles * tile;
         r.cfg.tile_recs = tile;
-        r.cfg.smem = 128 + (size_t)r.cfg.stages * tile * rec;
+        r.cfg.smem = 128 + (size_t)r.cfg.stages * tile * rec + term_bytes;
     }
     *pl = r;
     return EM_OK;

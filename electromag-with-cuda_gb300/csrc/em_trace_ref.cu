@@ -105,7 +105,7 @@ template <class T> struct Acc {
 // Adds the charges held in shared memory [0, count) to lane t's partial sum.
 template <class T, int TPL, int ARITH, class Rec>
 __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T px, T py, T pz,
-                                           T K, bool three_arg, bool nb, Acc<T> &a)
+                                           T K, bool three_arg, bool nb, float4 *xbuf, Acc<T> &a)
 {
     if (ARITH == ARITH_FAST2) {
         // charge pairs t, t+TPL, ... ; count is a multiple of 2*TPL; the tile
@@ -124,10 +124,16 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
         // TPL lanes per line: lane t forms the terms of charges j0 + u TPL + t
         // (eight per lane in flight, from the branch-free rounded operations,
         // redone with the compiler's rounded operations when an operand
-        // leaves its checked range); each round's TPL terms are broadcast from
-        // their lanes and every lane of the line adds them in charge order,
-        // so all of them hold the reference's sum (no reduction after).
-        // count is a multiple of 8 TPL (the padding granule).
+        // leaves its checked range); every lane of the line then takes each
+        // round's TPL terms in charge order and adds them, so all of them
+        // hold the reference's sum (no reduction after).  The terms travel
+        // by shuffles (4 lanes) or through the warp's term buffer xbuf (8
+        // lanes: one broadcast 16-byte load per charge instead of three
+        // shuffles), laid out [round][lane of the line][line] so that both
+        // the stores and the reads take whole wavefronts.  count is a
+        // multiple of 8 TPL (the padding granule).
+        constexpr int G = 32 / TPL; // lines per warp
+        const int g = (threadIdx.x & 31) / TPL;
         const int base = (threadIdx.x & 31) & ~(TPL - 1);
         for (int j0 = 0; j0 < count; j0 += 8 * TPL) {
             T tx[8], ty[8], tz[8];
@@ -148,13 +154,31 @@ __device__ __forceinline__ void accumulate(const Rec *tile, int count, int t, T 
                     tz[u] = ez;
                 }
             }
+            if constexpr (TPL >= kExactSmemTpl) {
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+                for (int u = 0; u < 8; ++u)
+                    xbuf[(u * TPL + t) * G + g] = make_float4(tx[u], ty[u], tz[u], 0.0f);
+                __syncwarp();
 #pragma unroll
-                for (int k = 0; k < TPL; ++k) {
-                    a.x = add_rn(a.x, __shfl_sync(0xffffffffu, tx[u], base + k));
-                    a.y = add_rn(a.y, __shfl_sync(0xffffffffu, ty[u], base + k));
-                    a.z = add_rn(a.z, __shfl_sync(0xffffffffu, tz[u], base + k));
+                for (int u = 0; u < 8; ++u) {
+#pragma unroll
+                    for (int k = 0; k < TPL; ++k) {
+                        const float4 v = xbuf[(u * TPL + k) * G + g];
+                        a.x = add_rn(a.x, v.x);
+                        a.y = add_rn(a.y, v.y);
+                        a.z = add_rn(a.z, v.z);
+                    }
+                }
+                __syncwarp(); // the buffer is rewritten by the next batch
+            } else {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+#pragma unroll
+                    for (int k = 0; k < TPL; ++k) {
+                        a.x = add_rn(a.x, __shfl_sync(0xffffffffu, tx[u], base + k));
+                        a.y = add_rn(a.y, __shfl_sync(0xffffffffu, ty[u], base + k));
+                        a.z = add_rn(a.z, __shfl_sync(0xffffffffu, tz[u], base + k));
+                    }
                 }
             }
         }
@@ -226,7 +250,7 @@ __device__ __forceinline__ void acc_finish(Acc<T> &a)
 template <class T, int TPL, int ARITH, int KL, class Rec>
 __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, const T *px,
                                              const T *py, const T *pz, T K, bool three_arg,
-                                             bool nb, Acc<T> *a)
+                                             bool nb, float4 *xbuf, Acc<T> *a)
 {
     if (ARITH == ARITH_FAST2 && KL > 1) {
         // a charge pair (two LDS.128) feeds KL lines, two charges per
@@ -248,7 +272,8 @@ __device__ __forceinline__ void accumulate_k(const Rec *tile, int count, int t, 
                 pair2_fast(PX[k], PY[k], PZ[k], A, B, a[k].X, a[k].Y, a[k].Z);
         }
     } else if (KL == 1) {
-        accumulate<T, TPL, ARITH>(tile, count, t, px[0], py[0], pz[0], K, three_arg, nb, a[0]);
+        accumulate<T, TPL, ARITH>(tile, count, t, px[0], py[0], pz[0], K, three_arg, nb, xbuf,
+                                  a[0]);
     } else {
 #pragma unroll 8
         for (int j = t; j < count; j += TPL) {
@@ -527,6 +552,12 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
     // exact arithmetic: the branch-free rounded operations once verified on
     // this device (else the compiler's rounded operations for every pair)
     const bool nb = ARITH == ARITH_EXACT && P.exact_nb != 0;
+    // exact arithmetic, 8 lanes per line: this warp's term buffer, after the
+    // charge tiles (the planner reserves it; other shapes never touch it)
+    float4 *xbuf = reinterpret_cast<float4 *>(
+                       smem + 128 +
+                       (size_t)(streamed ? P.stages * P.tile_recs : P.p_pad) * sizeof(Rec)) +
+                   (size_t)warp * (kExactTermBytesPerWarp / 16);
     const int t = lane % TPL;
     const size_t n = (size_t)P.n;
 
@@ -628,7 +659,7 @@ __global__ void __launch_bounds__(MAXT, 1) ref_trace_kernel(const RefTraceParams
                                               reinterpret_cast<const float *>(pz), hx, hy, hz,
                                               l2);
                 else
-                    accumulate_k<T, TPL, ARITH, KL>(tp, count, t, px, py, pz, K, three_arg, nb,
+                    accumulate_k<T, TPL, ARITH, KL>(tp, count, t, px, py, pz, K, three_arg, nb, xbuf,
                                                     acc);
             };
             if (!streamed) {
