@@ -15,7 +15,7 @@ against the oracle's restatement of the reference's SSE float path
 lane and warps per CTA never change a line's bits, so the subset's vertices
 are those the full benchmark computes for the same lines.
 
-Tolerances (the north-star's):
+Tolerances (the parity bar of the fast path against the reference):
 - vertices within 1e-4 relative of the reference for the first 500 steps,
   up to a line's first approach within 0.5 of a negative charge (the
   reference keeps stepping through charges, where trajectories turn
